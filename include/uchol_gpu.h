@@ -1,0 +1,169 @@
+/*
+ * uchol_gpu.h — device numeric phase of the MAGLA UCHOL direct solver on one
+ * GB300 (sm_103a): supernodal multifrontal U^T D U (= L D L^T) factorisation
+ * of a symmetric upper-CSR matrix, forward / diagonal / backward solves, the
+ * FP64 residual product and iterative refinement.
+ *
+ * This is the drop-in boundary: the managed MAGLA code keeps its public
+ * classes and replaces two internal calls with these entry points.
+ *
+ *   uchol_symbolic_create   uploads the integer output of
+ *       UtduSymbolicFactorization.Analyze (CAESolvers/UCHOL/UtduSymbolicFactorization.cs:240-295):
+ *       the permutation, PermutedSymmetricPattern arrays
+ *       (CAESolvers/UCHOL/PermutedSymmetricPattern.cs:41-72) and SupernodalStructure arrays
+ *       (CAESolvers/UCHOL/SupernodalStructure.cs:44-96).  Done once per sparsity pattern.
+ *   uchol_factorize         replaces SupernodalMultifrontalFactorizer.Factorize
+ *       (CAESolvers/UCHOL/UtduNumericFactorization.cs:281-403), called from
+ *       SymmetricUtduSolver.Factorize (CAESolvers/UCHOL/SymmetricUtduSolver.cs:95),
+ *       including EnsureCompatible (UtduSymbolicFactorization.cs:306-319).
+ *   uchol_factor_diagonal   UtduNumericFactorization.Diagonal (UtduNumericFactorization.cs:84).
+ *   uchol_solve             replaces the body of UtduNumericFactorization.Solve
+ *       (UtduNumericFactorization.cs:90-112), for nrhs columns at once.
+ *   uchol_residual_norms    UtduNumericFactorization.ResidualNorm (UtduNumericFactorization.cs:222-234)
+ *       and ResidualCalculator.CalculateResidualNorm (CAESolvers/ResidualCalculator.cs:5-20).
+ *   uchol_solve_refined     a low-precision factor plus FP64-residual refinement;
+ *       has no single counterpart in the reference (its solves are FP64 only).
+ *
+ * Conventions: every function returns a status (UCHOL_OK = 0, codes below);
+ * uchol_last_error() gives the message of the calling thread's last failure.
+ * Host pointers are only read during the call (the library copies them).
+ * Handles are not thread-safe for concurrent factorisations of the same
+ * symbolic handle; solves on one factor are serialised internally.
+ */
+#ifndef UCHOL_GPU_H
+#define UCHOL_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#ifndef UCHOL_OK
+#define UCHOL_OK 0
+#define UCHOL_BAD_ARG 1           /* ArgumentException / ArgumentNullException */
+#define UCHOL_PATTERN_MISMATCH 2  /* ArgumentException from EnsureCompatible */
+#define UCHOL_NOT_SPD 3           /* InvalidOperationException (pivot rejected, regularization off) */
+#define UCHOL_OOM 4               /* device memory exhausted (checked before any arithmetic) */
+#define UCHOL_TIMEOUT 5           /* a bounded device wait ran out */
+#define UCHOL_CUDA_ERROR 6
+#define UCHOL_TOO_DENSE 7         /* InvalidOperationException: front too large */
+#define UCHOL_NO_CONVERGENCE 8    /* refinement did not reach its tolerance */
+#define UCHOL_INTERNAL 9
+#endif
+
+typedef struct uchol_symbolic_s* uchol_symbolic;
+typedef struct uchol_factor_s* uchol_factor;
+
+/* Arithmetic of the factorisation. */
+#define UCHOL_PRECISION_FP64 0   /* FP64 fronts, FP64 Schur updates (plain form) */
+#define UCHOL_PRECISION_TF32 1   /* FP32 fronts, Schur GEMMs on tcgen05 kind::tf32, FP32 accumulation */
+#define UCHOL_PRECISION_BF16 2   /* FP32 fronts, Schur GEMMs on tcgen05 kind::f16 (BF16), FP32 accumulation */
+
+/* Integer output of the symbolic phase; array lengths in brackets. */
+typedef struct {
+    int n;                        /* Size */
+    int nnz;                      /* matrix NonZeroCount (upper half incl. diagonal) */
+    const int* row_ptr;           /* [n+1]  upper-CSR pattern of A (SymmetricCSRMatrix.RowPointers) */
+    const int* col;               /* [nnz]  SymmetricCSRMatrix.ColumnIndices */
+    const int* permutation;       /* [n]    UtduSymbolicFactorization.Permutation */
+    const int* diag_value_index;  /* [n]    PermutedSymmetricPattern.DiagonalValueIndices */
+    const int* pattern_ptr;       /* [n+1]  PermutedSymmetricPattern.Pointers */
+    const int* pattern_rows;      /* [pattern_ptr[n]] PermutedSymmetricPattern.Rows */
+    const int* lower_start;       /* [n]    PermutedSymmetricPattern.LowerStart */
+    const int* lower_value_ptr;   /* [n+1]  PermutedSymmetricPattern.LowerValuePointers */
+    const int* lower_value_index; /* [lower_value_ptr[n]] PermutedSymmetricPattern.LowerValueIndices */
+    int supernode_count;          /* SupernodalStructure.Count */
+    const int* first_column;      /* [count+1] SupernodalStructure.FirstColumn */
+    const int* parent;            /* [count]   SupernodalStructure.Parent */
+    const int* child_ptr;         /* [count+1] SupernodalStructure.ChildPointers */
+    const int* children;          /* [child_ptr[count]] SupernodalStructure.Children */
+    const int* front_ptr;         /* [count+1] SupernodalStructure.PatternPointers */
+    const int* front_rows;        /* [front_ptr[count]] SupernodalStructure.PatternRows */
+} uchol_symbolic_desc;
+
+/* UtduSolverOptions (CAESolvers/UCHOL/UtduSymbolicFactorization.cs:31-98), numeric part. */
+typedef struct {
+    int allow_diagonal_regularization;  /* AllowDiagonalRegularization (default 1) */
+    double pivot_tolerance;             /* PivotTolerance (default 1e-13) */
+    double diagonal_regularization;     /* DiagonalRegularization (default 1e-10) */
+    int panel_width;                    /* PanelWidth, clamped to 4..128: FP64 pivot-block width */
+    int precision;                      /* UCHOL_PRECISION_* */
+    int block_width;                    /* outer block of the tensor-core Schur GEMM (0 = tuned) */
+} uchol_options;
+
+/* Pivot statistics (UtduNumericFactorization.cs:57-84) and timings. */
+typedef struct {
+    int regularized_pivot_count;
+    int negative_pivot_count;
+    double smallest_pivot_magnitude;
+    double largest_pivot_magnitude;
+    int failed_pivot;       /* elimination-order index of a rejected pivot (strict mode), else -1 */
+    double factor_ms;       /* device time of the numeric factorisation (CUDA events) */
+    int64_t device_bytes;   /* device memory held by the factor */
+} uchol_factor_stats;
+
+typedef struct {
+    double tolerance;       /* target ||b - A x||_2 / ||b||_2 per column (e.g. 1e-10) */
+    int max_iterations;     /* refinement steps after the first solve */
+    int method;             /* 0 = automatic, 1 = classical refinement, 2 = factor-preconditioned CG */
+} uchol_refine_options;
+
+typedef struct {
+    int iterations;             /* refinement steps taken (max over columns) */
+    double relative_residual;   /* final max over columns of ||b - A x|| / ||b|| (FP64) */
+    double initial_relative_residual;
+    double solve_ms;            /* device time of the whole solve / refinement */
+} uchol_refine_stats;
+
+void uchol_default_options(uchol_options* o);
+
+int uchol_symbolic_create(const uchol_symbolic_desc* desc, uchol_symbolic* out);
+int uchol_symbolic_destroy(uchol_symbolic s);
+/* Streams: all work of a symbolic handle and its factors runs on this CUDA stream
+ * (cudaStream_t passed as void*; NULL = a private stream created by the library). */
+int uchol_symbolic_set_stream(uchol_symbolic s, void* stream);
+
+/* Numeric factorisation from host values [nnz] (SymmetricCSRMatrix.Values order). */
+int uchol_factorize(uchol_symbolic s, int n, int nnz, const double* values, const uchol_options* opts,
+                    uchol_factor* out, uchol_factor_stats* stats);
+/* Same with the values already resident in device memory. */
+int uchol_factorize_device(uchol_symbolic s, int n, int nnz, const double* d_values, const uchol_options* opts,
+                           uchol_factor* out, uchol_factor_stats* stats);
+/* Refactorise an existing factor in place with new values (same pattern, same options). */
+int uchol_refactorize(uchol_factor f, const double* values, int on_device, uchol_factor_stats* stats);
+int uchol_factor_destroy(uchol_factor f);
+
+int uchol_factor_diagonal(uchol_factor f, double* out_n);
+int uchol_factor_get_stats(uchol_factor f, uchol_factor_stats* stats);
+
+/* X = A^-1 B for nrhs columns (column-major, leading dimension ld >= n), host
+ * buffers, original equation order; one pass of the factor (no refinement). */
+int uchol_solve(uchol_factor f, int n, int nrhs, const double* b, int ldb, double* x, int ldx);
+/* Device-buffer variant. */
+int uchol_solve_device(uchol_factor f, int n, int nrhs, const double* d_b, int ldb, double* d_x, int ldx);
+/* Solve with FP64-residual refinement against the factorised matrix. */
+int uchol_solve_refined(uchol_factor f, int n, int nrhs, const double* b, int ldb, double* x, int ldx,
+                        const uchol_refine_options* ro, uchol_refine_stats* rs);
+int uchol_solve_refined_device(uchol_factor f, int n, int nrhs, const double* d_b, int ldb, double* d_x, int ldx,
+                               const uchol_refine_options* ro, uchol_refine_stats* rs);
+
+/* ||b_j - A x_j||_2 for each column j with the FP64 symmetric product of the
+ * factorised values (host buffers); out_norms[nrhs]. */
+int uchol_residual_norms(uchol_factor f, int n, int nrhs, const double* b, int ldb, const double* x, int ldx,
+                         double* out_norms);
+
+/* Device-time of the last call on the handle's stream, per phase. */
+typedef struct {
+    double assemble_ms, extend_add_ms, small_fronts_ms, panel_ms, schur_ms, total_ms;
+    int launches;            /* kernel launches of the last factorisation */
+} uchol_phase_times;
+int uchol_factor_phase_times(uchol_factor f, uchol_phase_times* t);
+
+const char* uchol_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* UCHOL_GPU_H */

@@ -1,0 +1,908 @@
+// C-ABI of the device numeric phase (include/uchol_gpu.h): symbolic upload,
+// plan cache, arena allocation, launch sequencing of the factorisation, the
+// solves and the FP64-residual refinement.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../../include/uchol_gpu.h"
+#include "factor_kernels.cuh"
+#include "plan.hpp"
+#include "solve_kernels.cuh"
+#include "tc_gemm.cuh"
+
+using namespace uchol_dev;
+
+namespace {
+
+thread_local std::string g_error;
+
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+void check(cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return;
+    if (e == cudaErrorMemoryAllocation) {
+        cudaGetLastError();
+        throw Error(UCHOL_OOM, std::string(what) + ": device memory exhausted");
+    }
+    throw Error(UCHOL_CUDA_ERROR, std::string(what) + ": " + cudaGetErrorString(e));
+}
+#define CK(call) check((call), #call)
+
+template <class F>
+int guarded(F&& f) {
+    try {
+        f();
+        g_error.clear();
+        return UCHOL_OK;
+    } catch (const Error& e) {
+        g_error = e.what();
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        g_error = "host allocation failed";
+        return UCHOL_OOM;
+    } catch (const std::exception& e) {
+        g_error = e.what();
+        return UCHOL_INTERNAL;
+    }
+}
+
+// Owning device allocation.
+struct DBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    DBuf() = default;
+    DBuf(const DBuf&) = delete;
+    DBuf& operator=(const DBuf&) = delete;
+    ~DBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    void alloc(size_t b, const char* what) {
+        release();
+        if (b == 0) b = 16;
+        cudaError_t e = cudaMalloc(&p, b);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            p = nullptr;
+            throw Error(UCHOL_OOM, std::string("cudaMalloc of ") + std::to_string(b) + " bytes for " + what +
+                                       " failed: " + cudaGetErrorString(e));
+        }
+        bytes = b;
+    }
+    template <class V>
+    void upload(const std::vector<V>& v, cudaStream_t s, const char* what) {
+        alloc(v.size() * sizeof(V), what);
+        if (!v.empty()) CK(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(V), cudaMemcpyHostToDevice, s));
+    }
+    template <class V>
+    V* as() const { return static_cast<V*>(p); }
+};
+
+struct DevPlan {
+    Plan plan;
+    DBuf sn, rel, asm_pos, zero_off, zero_len, ea_items, ea_entries, small, pivot_tasks, panel_tasks, simt_tasks, tc_tasks;
+    DBuf fvec_off, solve_fronts, solve_tasks;
+};
+
+inline int grid_for(long long work, int block, int cap = 152 * 16) {
+    long long g = (work + block - 1) / block;
+    return (int)std::max<long long>(1, std::min<long long>(g, cap));
+}
+
+}  // namespace
+
+struct uchol_symbolic_s {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int n = 0, nnz = 0, count = 0;
+    // host copies of the symbolic arrays (plans are built lazily per configuration)
+    std::vector<int> row_ptr, col, perm, diag_idx, pat_ptr, pat_rows, lower_start, lower_ptr, lower_idx;
+    std::vector<int> first_col, parent, child_ptr, children, front_ptr, front_rows;
+    DBuf d_perm, d_diag_idx, d_rows, d_child_ptr, d_children, d_full_ptr, d_full_col, d_full_src;
+    long long full_nnz = 0;
+    std::map<std::string, std::unique_ptr<DevPlan>> plans;
+    std::mutex mu;
+
+    DevPlan* get_plan(const PlanConfig& c) {
+        std::string key = std::to_string(c.pivot_block) + "/" + std::to_string(c.outer_block) + "/" +
+                          std::to_string(c.small_max) + "/" + std::to_string(c.tensor_core);
+        auto it = plans.find(key);
+        if (it != plans.end()) return it->second.get();
+        auto dp = std::make_unique<DevPlan>();
+        try {
+            dp->plan = build_plan(n, count, first_col.data(), parent.data(), child_ptr.data(), children.data(),
+                                  front_ptr.data(), front_rows.data(), diag_idx.data(), pat_ptr.data(), pat_rows.data(),
+                                  lower_start.data(), lower_ptr.data(), lower_idx.data(), nnz, c);
+        } catch (const std::runtime_error& e) {
+            throw Error(UCHOL_BAD_ARG, std::string("inconsistent symbolic factorization: ") + e.what());
+        }
+        const Plan& P = dp->plan;
+        dp->sn.upload(P.sn, stream, "supernode table");
+        dp->rel.upload(P.rel, stream, "relative indices");
+        dp->asm_pos.upload(P.assemble_pos, stream, "assembly map");
+        dp->zero_off.upload(P.zero_off, stream, "plan");
+        dp->zero_len.upload(P.zero_len, stream, "plan");
+        dp->ea_items.upload(P.ea_items, stream, "plan");
+        dp->ea_entries.upload(P.ea_entries, stream, "plan");
+        dp->small.upload(P.small_fronts, stream, "plan");
+        dp->pivot_tasks.upload(P.pivot_tasks, stream, "plan");
+        dp->panel_tasks.upload(P.panel_tasks, stream, "plan");
+        dp->simt_tasks.upload(P.simt_tasks, stream, "plan");
+        dp->tc_tasks.upload(P.tc_tasks, stream, "plan");
+        dp->fvec_off.upload(P.fvec_off, stream, "plan");
+        dp->solve_fronts.upload(P.solve_fronts, stream, "plan");
+        dp->solve_tasks.upload(P.solve_tasks, stream, "plan");
+        CK(cudaStreamSynchronize(stream));
+        DevPlan* raw = dp.get();
+        plans[key] = std::move(dp);
+        return raw;
+    }
+};
+
+struct uchol_factor_s {
+    uchol_symbolic sym = nullptr;
+    DevPlan* dp = nullptr;
+    uchol_options opts{};
+    int precision = UCHOL_PRECISION_FP64;
+    size_t elem = 8;              // bytes per front element
+    DBuf panel, contrib, stage_a, stage_b, diag, values, full_val, stats, ctl;
+    DBuf work, fv, vec[6], scal;   // solve workspace
+    int ws_nrhs = 0;
+    TcMaps maps;
+    uchol_factor_stats last{};
+    uchol_phase_times phases{};
+    std::mutex mu;
+};
+
+namespace {
+
+struct StreamTimer {
+    cudaEvent_t a = nullptr, b = nullptr;
+    cudaStream_t s;
+    explicit StreamTimer(cudaStream_t st) : s(st) {
+        CK(cudaEventCreate(&a));
+        CK(cudaEventCreate(&b));
+        CK(cudaEventRecord(a, s));
+    }
+    double stop() {
+        CK(cudaEventRecord(b, s));
+        CK(cudaEventSynchronize(b));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, a, b));
+        return ms;
+    }
+    ~StreamTimer() {
+        if (a) cudaEventDestroy(a);
+        if (b) cudaEventDestroy(b);
+    }
+};
+
+PlanConfig config_for(const uchol_options& o) {
+    PlanConfig c;
+    c.pivot_block = std::min(kMaxPivotBlock, std::max(4, std::min(128, o.panel_width)));
+    if (o.precision == UCHOL_PRECISION_FP64) {
+        c.tensor_core = false;
+        c.outer_block = c.pivot_block;
+    } else {
+        c.tensor_core = true;
+        c.pivot_block = std::min(c.pivot_block, 32);
+        int nb = o.block_width > 0 ? o.block_width : 128;
+        // whole-K staging in shared memory: at most 4 blocks of 128 bytes per operand row
+        const int nb_max = o.precision == UCHOL_PRECISION_BF16 ? 256 : 128;
+        nb = std::max(64, std::min(nb_max, nb / 64 * 64));
+        // the outer block must be a multiple of the pivot block
+        nb = nb / c.pivot_block * c.pivot_block;
+        c.outer_block = nb;
+    }
+    return c;
+}
+
+template <class T>
+void run_factor_launches(uchol_factor_s* F, cudaStream_t st) {
+    DevPlan& D = *F->dp;
+    const Plan& P = D.plan;
+    T* panel = F->panel.as<T>();
+    T* contrib = F->contrib.as<T>();
+    double* diag = F->diag.as<double>();
+    PivotStats* stats = F->stats.as<PivotStats>();
+    FactorCtl* ctl = F->ctl.as<FactorCtl>();
+    const SnDev* sn = D.sn.as<SnDev>();
+    int launches = 0;
+    size_t small_smem = (size_t)P.max_small_m * P.max_small_m * sizeof(double);
+    if (small_smem > 48 * 1024)
+        CK(cudaFuncSetAttribute(k_small_fronts<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)small_smem));
+    for (const Launch& L : P.launches) {
+        switch (L.kind) {
+            case Launch::ZeroContrib: {
+                dim3 g(64, std::min(L.count, 65535));
+                k_zero_ranges<T><<<g, 256, 0, st>>>(D.zero_off.as<long long>() + L.begin,
+                                                     D.zero_len.as<long long>() + L.begin, L.count, contrib);
+                break;
+            }
+            case Launch::ExtendAdd:
+                k_extend_add<T><<<(L.count + 7) / 8, 256, 0, st>>>(D.ea_items.as<EaItem>() + L.begin, L.count,
+                                                                   D.ea_entries.as<EaEntry>(), sn, D.rel.as<int>(),
+                                                                   panel, contrib);
+                break;
+            case Launch::SmallFronts:
+                k_small_fronts<T><<<L.count, 256, small_smem, st>>>(D.small.as<int>() + L.begin, sn, panel, contrib,
+                                                                    diag, ctl, stats);
+                break;
+            case Launch::PivotBlock:
+                k_pivot_block<T><<<L.count, 128, 0, st>>>(D.pivot_tasks.as<PanelTask>() + L.begin, sn, panel, diag, ctl,
+                                                          stats);
+                break;
+            case Launch::Trsm: {
+                const PanelTask* tk = D.panel_tasks.as<PanelTask>() + L.begin;
+                if (F->precision == UCHOL_PRECISION_BF16)
+                    k_trsm<T, __nv_bfloat16, float, 32><<<L.count, 128, 0, st>>>(
+                        tk, sn, panel, diag, F->stage_a.as<__nv_bfloat16>(), F->stage_b.as<__nv_bfloat16>(),
+                        P.cfg.outer_block);
+                else if (F->precision == UCHOL_PRECISION_TF32)
+                    k_trsm<T, float, float, 32><<<L.count, 128, 0, st>>>(tk, sn, panel, diag, F->stage_a.as<float>(),
+                                                                          F->stage_b.as<float>(), P.cfg.outer_block);
+                else if (P.cfg.pivot_block <= 32)
+                    k_trsm<T, T, double, 32><<<L.count, 128, 0, st>>>(tk, sn, panel, diag, nullptr, nullptr, 0);
+                else
+                    k_trsm<T, T, double, 64><<<L.count, 128, 0, st>>>(tk, sn, panel, diag, nullptr, nullptr, 0);
+                break;
+            }
+            case Launch::SimtUpdate:
+                if (sizeof(T) == 8)
+                    k_simt_update<T, double><<<L.count, 256, 0, st>>>(D.simt_tasks.as<TileTask>() + L.begin, sn, panel,
+                                                                      contrib, diag);
+                else
+                    k_simt_update<T, float><<<L.count, 256, 0, st>>>(D.simt_tasks.as<TileTask>() + L.begin, sn, panel,
+                                                                     contrib, diag);
+                break;
+            case Launch::TcUpdate:
+                launch_tc_update(F->precision == UCHOL_PRECISION_BF16, D.tc_tasks.as<TileTask>() + L.begin, L.count, sn,
+                                 (float*)panel, (float*)contrib, F->maps, P.cfg.outer_block, &stats->status, st);
+                break;
+        }
+        ++launches;
+    }
+    CK(cudaGetLastError());
+    F->phases.launches = launches;
+}
+
+// Full-matrix product structure (both triangles) for the FP64 residual.
+void build_full_csr(uchol_symbolic_s* S) {
+    const int n = S->n;
+    std::vector<int> cnt(n + 1, 0);
+    for (int r = 0; r < n; ++r)
+        for (int k = S->row_ptr[r]; k < S->row_ptr[r + 1]; ++k) {
+            int c = S->col[k];
+            cnt[r + 1]++;
+            if (c != r) cnt[c + 1]++;
+        }
+    for (int i = 0; i < n; ++i) cnt[i + 1] += cnt[i];
+    std::vector<int> fcol(cnt[n]), fsrc(cnt[n]);
+    std::vector<int> fill(cnt.begin(), cnt.end() - 1);
+    for (int r = 0; r < n; ++r)
+        for (int k = S->row_ptr[r]; k < S->row_ptr[r + 1]; ++k) {
+            int c = S->col[k];
+            fcol[fill[r]] = c;
+            fsrc[fill[r]++] = k;
+            if (c != r) {
+                fcol[fill[c]] = r;
+                fsrc[fill[c]++] = k;
+            }
+        }
+    S->full_nnz = cnt[n];
+    S->d_full_ptr.upload(cnt, S->stream, "product structure");
+    S->d_full_col.upload(fcol, S->stream, "product structure");
+    S->d_full_src.upload(fsrc, S->stream, "product structure");
+}
+
+void factorize_impl(uchol_factor_s* F, const double* values, bool on_device) {
+    uchol_symbolic_s* S = F->sym;
+    cudaStream_t st = S->stream;
+    const Plan& P = F->dp->plan;
+    StreamTimer total(st);
+    if (on_device)
+        CK(cudaMemcpyAsync(F->values.p, values, (size_t)S->nnz * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    else
+        CK(cudaMemcpyAsync(F->values.p, values, (size_t)S->nnz * sizeof(double), cudaMemcpyHostToDevice, st));
+    PivotStats* stats = F->stats.as<PivotStats>();
+    CK(cudaMemsetAsync(stats, 0, sizeof(PivotStats), st));
+    if (S->n > 0) {
+        k_diag_scale<<<grid_for(S->n, 256), 256, 0, st>>>(F->values.as<double>(), S->d_diag_idx.as<int>(), S->n, stats);
+    }
+    k_finish_scale<<<1, 1, 0, st>>>(stats, F->ctl.as<FactorCtl>(), F->opts.pivot_tolerance,
+                                    F->opts.diagonal_regularization, F->opts.allow_diagonal_regularization);
+    if (S->full_nnz > 0)
+        k_gather_values<<<grid_for(S->full_nnz, 256), 256, 0, st>>>(F->values.as<double>(), S->d_full_src.as<int>(),
+                                                                     S->full_nnz, F->full_val.as<double>());
+    if (S->count > 0) {
+        CK(cudaMemsetAsync(F->panel.p, 0, F->panel.bytes, st));
+        if (F->elem == 8)
+            k_assemble<double><<<grid_for(S->nnz, 256), 256, 0, st>>>(F->values.as<double>(), F->dp->asm_pos.as<long long>(),
+                                                                      S->nnz, F->panel.as<double>());
+        else
+            k_assemble<float><<<grid_for(S->nnz, 256), 256, 0, st>>>(F->values.as<double>(), F->dp->asm_pos.as<long long>(),
+                                                                     S->nnz, F->panel.as<float>());
+        if (F->elem == 8) run_factor_launches<double>(F, st);
+        else run_factor_launches<float>(F, st);
+    }
+    PivotStats hs;
+    CK(cudaMemcpyAsync(&hs, stats, sizeof(PivotStats), cudaMemcpyDeviceToHost, st));
+    double ms = total.stop();
+    (void)P;
+    uchol_factor_stats& o = F->last;
+    o.regularized_pivot_count = hs.regularized;
+    o.negative_pivot_count = hs.negative;
+    o.smallest_pivot_magnitude = S->count ? __builtin_bit_cast(double, hs.min_bits) : 0.0;
+    o.largest_pivot_magnitude = S->count ? __builtin_bit_cast(double, hs.max_bits) : 0.0;
+    if (S->count == 0) o.smallest_pivot_magnitude = o.largest_pivot_magnitude = 0.0;
+    o.failed_pivot = hs.failed == INT_MAX ? -1 : hs.failed;
+    o.factor_ms = ms;
+    o.device_bytes = (int64_t)(F->panel.bytes + F->contrib.bytes + F->stage_a.bytes + F->stage_b.bytes + F->diag.bytes +
+                               F->values.bytes + F->full_val.bytes);
+    F->phases.total_ms = ms;
+    if (hs.status != 0)
+        throw Error(UCHOL_TIMEOUT, "a bounded device wait expired during the factorization (status " +
+                                       std::to_string(hs.status) + ")");
+    if (o.failed_pivot >= 0)
+        throw Error(UCHOL_NOT_SPD, "Pivot in equation " + std::to_string(o.failed_pivot) +
+                                       " (in elimination order) is not positive: the matrix is not positive definite. "
+                                       "Enable diagonal regularization if factorization must be completed.");
+}
+
+void check_options(const uchol_options* o) {
+    if (!o) return;
+    if (o->precision < UCHOL_PRECISION_FP64 || o->precision > UCHOL_PRECISION_BF16)
+        throw Error(UCHOL_BAD_ARG, "unknown precision mode");
+    if (!(o->pivot_tolerance >= 0.0) || !(o->diagonal_regularization > 0.0))
+        throw Error(UCHOL_BAD_ARG, "pivot tolerance must be >= 0 and regularization > 0");
+}
+
+uchol_factor_s* create_factor(uchol_symbolic_s* S, int n, int nnz, const uchol_options* opts) {
+    if (!S) throw Error(UCHOL_BAD_ARG, "symbolic handle is null");
+    if (n != S->n)
+        throw Error(UCHOL_PATTERN_MISMATCH, "Matrix size " + std::to_string(n) +
+                                                " does not match the symbolic factorization built for " +
+                                                std::to_string(S->n) + " equations.");
+    if (nnz != S->nnz)
+        throw Error(UCHOL_PATTERN_MISMATCH,
+                    "The matrix sparse structure has changed since symbolic analysis (previously " +
+                        std::to_string(S->nnz) + " nonzero elements, now " + std::to_string(nnz) +
+                        "). Symbolic factorization can be reused only when the structure is unchanged. Run Analyze again.");
+    check_options(opts);
+    auto F = std::make_unique<uchol_factor_s>();
+    F->sym = S;
+    if (opts) F->opts = *opts; else uchol_default_options(&F->opts);
+    F->precision = F->opts.precision;
+    F->elem = F->precision == UCHOL_PRECISION_FP64 ? 8 : 4;
+    PlanConfig cfg = config_for(F->opts);
+    F->dp = S->get_plan(cfg);
+    const Plan& P = F->dp->plan;
+    cudaStream_t st = S->stream;
+    F->panel.alloc((size_t)P.factor_elems * F->elem, "factor panels");
+    F->contrib.alloc((size_t)P.contrib_elems * F->elem, "contribution blocks");
+    if (cfg.tensor_core && P.stage_rows > 0) {
+        size_t op = F->precision == UCHOL_PRECISION_BF16 ? 2 : 4;
+        F->stage_a.alloc((size_t)P.stage_rows * cfg.outer_block * op, "operand staging");
+        F->stage_b.alloc((size_t)P.stage_rows * cfg.outer_block * op, "operand staging");
+        CK(cudaMemsetAsync(F->stage_a.p, 0, F->stage_a.bytes, st));
+        CK(cudaMemsetAsync(F->stage_b.p, 0, F->stage_b.bytes, st));
+        F->maps = make_tc_maps(F->precision == UCHOL_PRECISION_BF16, F->stage_a.p, F->stage_b.p, P.stage_rows,
+                               cfg.outer_block);
+    }
+    F->diag.alloc((size_t)std::max(1, S->n) * sizeof(double), "pivots");
+    F->values.alloc((size_t)std::max(1, S->nnz) * sizeof(double), "matrix values");
+    F->full_val.alloc((size_t)std::max<long long>(1, S->full_nnz) * sizeof(double), "matrix values");
+    F->stats.alloc(sizeof(PivotStats), "statistics");
+    F->ctl.alloc(sizeof(FactorCtl), "statistics");
+    return F.release();
+}
+
+// ---- solves ----
+
+template <class T, class Cv>
+void run_solve(uchol_factor_s* F, int nrhs, Cv* work, Cv* fv) {
+    uchol_symbolic_s* S = F->sym;
+    DevPlan& D = *F->dp;
+    const Plan& P = D.plan;
+    cudaStream_t st = S->stream;
+    SolveArgs A;
+    A.sn = D.sn.as<SnDev>();
+    A.rel = D.rel.as<int>();
+    A.rows = S->d_rows.as<int>();
+    A.child_ptr = S->d_child_ptr.as<int>();
+    A.children = S->d_children.as<int>();
+    A.fvec_off = D.fvec_off.as<long long>();
+    A.fv_stride = P.fvec_elems;
+    A.n = S->n;
+    A.nrhs = nrhs;
+    A.ldw = S->n;
+    const T* panel = F->panel.as<T>();
+    const int* fronts = D.solve_fronts.as<int>();
+    const SolveBlockTask* tasks = D.solve_tasks.as<SolveBlockTask>();
+    const double* diag = F->diag.as<double>();
+    for (const SolveLaunch& L : P.fwd_launches) {
+        if (L.count == 0) continue;
+        switch (L.kind) {
+            case SolveLaunch::FwdGather: k_fwd_gather<Cv><<<L.count, 128, 0, st>>>(fronts + L.begin, A, work, fv); break;
+            case SolveLaunch::FwdDiag: k_fwd_diag<T, Cv><<<L.count, 64, 0, st>>>(tasks + L.begin, A, panel, fv); break;
+            case SolveLaunch::FwdRows: k_fwd_rows<T, Cv><<<L.count, 128, 0, st>>>(tasks + L.begin, A, panel, fv); break;
+            case SolveLaunch::FwdFinish: k_fwd_finish<Cv><<<L.count, 128, 0, st>>>(fronts + L.begin, A, diag, fv, work); break;
+            default: break;
+        }
+    }
+    for (const SolveLaunch& L : P.bwd_launches) {
+        if (L.count == 0) continue;
+        switch (L.kind) {
+            case SolveLaunch::BwdGather: k_bwd_gather<Cv><<<L.count, 128, 0, st>>>(fronts + L.begin, A, work, fv); break;
+            case SolveLaunch::BwdTail:
+            case SolveLaunch::BwdCols: k_bwd_cols<T, Cv><<<L.count, 256, 0, st>>>(tasks + L.begin, A, panel, fv); break;
+            case SolveLaunch::BwdDiag: k_bwd_diag<T, Cv><<<L.count, 64, 0, st>>>(tasks + L.begin, A, panel, fv); break;
+            case SolveLaunch::BwdFinish: k_bwd_finish<Cv><<<L.count, 128, 0, st>>>(fronts + L.begin, A, fv, work); break;
+            default: break;
+        }
+    }
+    CK(cudaGetLastError());
+}
+
+void ensure_workspace(uchol_factor_s* F, int nrhs) {
+    if (F->ws_nrhs >= nrhs) return;
+    uchol_symbolic_s* S = F->sym;
+    const Plan& P = F->dp->plan;
+    size_t cv = F->precision == UCHOL_PRECISION_FP64 ? 8 : 4;
+    F->work.alloc((size_t)std::max(1, S->n) * nrhs * cv, "solve workspace");
+    F->fv.alloc((size_t)P.fvec_elems * nrhs * cv, "solve workspace");
+    for (auto& v : F->vec) v.alloc((size_t)std::max(1, S->n) * nrhs * sizeof(double), "refinement vectors");
+    F->scal.alloc((size_t)(kDotBlocks * nrhs + 16 * nrhs) * sizeof(double), "refinement scalars");
+    F->ws_nrhs = nrhs;
+}
+
+// x = A^-1 b through the factor only (device buffers, original order).
+void apply_factor(uchol_factor_s* F, int nrhs, const double* b, int ldb, double* x, int ldx) {
+    uchol_symbolic_s* S = F->sym;
+    cudaStream_t st = S->stream;
+    const int n = S->n;
+    if (n == 0) return;
+    dim3 g(grid_for(n, 256, 1024), std::min(nrhs, 65535));
+    if (F->precision == UCHOL_PRECISION_FP64) {
+        double* work = F->work.as<double>();
+        k_permute_in<double><<<g, 256, 0, st>>>(b, ldb, S->d_perm.as<int>(), n, nrhs, work, n);
+        if (S->count) run_solve<double, double>(F, nrhs, work, F->fv.as<double>());
+        k_permute_out<double><<<g, 256, 0, st>>>(work, n, S->d_perm.as<int>(), n, nrhs, x, ldx);
+    } else {
+        float* work = F->work.as<float>();
+        k_permute_in<float><<<g, 256, 0, st>>>(b, ldb, S->d_perm.as<int>(), n, nrhs, work, n);
+        if (S->count) run_solve<float, float>(F, nrhs, work, F->fv.as<float>());
+        k_permute_out<float><<<g, 256, 0, st>>>(work, n, S->d_perm.as<int>(), n, nrhs, x, ldx);
+    }
+    CK(cudaGetLastError());
+}
+
+void residual(uchol_factor_s* F, int nrhs, const double* x, int ldx, const double* b, int ldb, double* r, int ldr) {
+    uchol_symbolic_s* S = F->sym;
+    if (S->n == 0) return;
+    k_spmv_residual<<<(S->n + 7) / 8, 256, 0, S->stream>>>(S->d_full_ptr.as<int>(), S->d_full_col.as<int>(),
+                                                          F->full_val.as<double>(), S->n, nrhs, x, ldx, b, ldb, r, ldr);
+}
+
+// out[r] = u_r . v_r (deterministic two-stage reduction) on the device.
+void dots(uchol_factor_s* F, int nrhs, const double* u, int ldu, const double* v, int ldv, double* out) {
+    uchol_symbolic_s* S = F->sym;
+    double* partial = F->scal.as<double>();
+    dim3 g(kDotBlocks, nrhs);
+    k_dot_partial<<<g, 256, 0, S->stream>>>(u, ldu, v, ldv, S->n, partial);
+    k_dot_finish<<<1, 32 * ((nrhs + 31) / 32), 0, S->stream>>>(partial, kDotBlocks, nrhs, out);
+}
+
+__global__ void k_fill(double* p, double v, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = v;
+}
+
+__global__ void k_cg_scalars(const double* num, const double* den, double* out, int nrhs) {
+    int r = threadIdx.x;
+    if (r < nrhs) out[r] = den[r] != 0.0 ? num[r] / den[r] : 0.0;
+}
+
+void solve_refined(uchol_factor_s* F, int nrhs, const double* b, int ldb, double* x, int ldx,
+                   const uchol_refine_options* ro, uchol_refine_stats* rs) {
+    uchol_symbolic_s* S = F->sym;
+    cudaStream_t st = S->stream;
+    const int n = S->n;
+    ensure_workspace(F, nrhs);
+    StreamTimer timer(st);
+    uchol_refine_options opt{1e-10, 50, 0};
+    if (ro) opt = *ro;
+    int method = opt.method;
+    if (method == 0)
+        method = (F->precision == UCHOL_PRECISION_FP64 || F->last.regularized_pivot_count > 0) ? 1 : 2;
+    if (n == 0) {
+        if (rs) *rs = {0, 0.0, 0.0, timer.stop()};
+        return;
+    }
+    double* r = F->vec[0].as<double>();
+    double* z = F->vec[1].as<double>();
+    double* p = F->vec[2].as<double>();
+    double* q = F->vec[3].as<double>();
+    double* sc = F->scal.as<double>() + kDotBlocks * nrhs;   // scalar area: 16 * nrhs doubles
+    double* bnorm2 = sc, *rnorm2 = sc + nrhs, *rz = sc + 2 * nrhs, *rz_new = sc + 3 * nrhs, *pq = sc + 4 * nrhs;
+    double* alpha = sc + 5 * nrhs, *beta = sc + 6 * nrhs;
+    std::vector<double> hb(nrhs), hr(nrhs);
+    dots(F, nrhs, b, ldb, b, ldb, bnorm2);
+    CK(cudaMemcpyAsync(hb.data(), bnorm2, nrhs * sizeof(double), cudaMemcpyDeviceToHost, st));
+    auto rel_max = [&]() {
+        CK(cudaMemcpyAsync(hr.data(), rnorm2, nrhs * sizeof(double), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        double worst = 0.0;
+        for (int j = 0; j < nrhs; ++j) {
+            double nb = std::sqrt(hb[j]), nr = std::sqrt(hr[j]);
+            worst = std::max(worst, nb > 0.0 ? nr / nb : nr);
+        }
+        return worst;
+    };
+    dim3 g(grid_for(n, 256, 1024), nrhs);
+    int it = 0;
+    double initial = 0.0, current = 0.0;
+    // x0 = M^-1 b
+    apply_factor(F, nrhs, b, ldb, x, ldx);
+    residual(F, nrhs, x, ldx, b, ldb, r, n);
+    dots(F, nrhs, r, n, r, n, rnorm2);
+    initial = current = rel_max();
+    if (method == 1) {
+        double* ones = sc + 15 * nrhs;
+        k_fill<<<(nrhs + 31) / 32, 32, 0, st>>>(ones, 1.0, nrhs);
+        while (current > opt.tolerance && it < opt.max_iterations) {
+            apply_factor(F, nrhs, r, n, z, n);
+            k_axpy_cols<<<g, 256, 0, st>>>(x, ldx, z, n, ones, 1.0, n, nrhs);
+            residual(F, nrhs, x, ldx, b, ldb, r, n);
+            dots(F, nrhs, r, n, r, n, rnorm2);
+            current = rel_max();
+            ++it;
+        }
+    } else {
+        // Conjugate gradients on A preconditioned by the factor, started from x0.
+        apply_factor(F, nrhs, r, n, z, n);
+        CK(cudaMemcpyAsync(p, z, (size_t)n * nrhs * sizeof(double), cudaMemcpyDeviceToDevice, st));
+        dots(F, nrhs, r, n, z, n, rz);
+        while (current > opt.tolerance && it < opt.max_iterations) {
+            residual(F, nrhs, p, n, nullptr, 0, q, n);   // q = A p
+            dots(F, nrhs, p, n, q, n, pq);
+            k_cg_scalars<<<1, 32 * ((nrhs + 31) / 32), 0, st>>>(rz, pq, alpha, nrhs);
+            k_axpy_cols<<<g, 256, 0, st>>>(x, ldx, p, n, alpha, 1.0, n, nrhs);
+            k_axpy_cols<<<g, 256, 0, st>>>(r, n, q, n, alpha, -1.0, n, nrhs);
+            ++it;
+            // true residual for the stopping test (FP64 product, no drift)
+            residual(F, nrhs, x, ldx, b, ldb, z, n);
+            dots(F, nrhs, z, n, z, n, rnorm2);
+            current = rel_max();
+            if (current <= opt.tolerance) break;
+            apply_factor(F, nrhs, r, n, z, n);
+            dots(F, nrhs, r, n, z, n, rz_new);
+            k_cg_scalars<<<1, 32 * ((nrhs + 31) / 32), 0, st>>>(rz_new, rz, beta, nrhs);
+            k_xpby_cols<<<g, 256, 0, st>>>(z, n, p, n, beta, n, nrhs);
+            CK(cudaMemcpyAsync(rz, rz_new, nrhs * sizeof(double), cudaMemcpyDeviceToDevice, st));
+        }
+    }
+    CK(cudaGetLastError());
+    double ms = timer.stop();
+    if (rs) *rs = {it, current, initial, ms};
+    if (current > opt.tolerance)
+        throw Error(UCHOL_NO_CONVERGENCE, "refinement stopped at relative residual " + std::to_string(current) +
+                                              " after " + std::to_string(it) + " steps (target " +
+                                              std::to_string(opt.tolerance) + ")");
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* uchol_last_error(void) { return g_error.c_str(); }
+
+void uchol_default_options(uchol_options* o) {
+    if (!o) return;
+    o->allow_diagonal_regularization = 1;
+    o->pivot_tolerance = 1e-13;
+    o->diagonal_regularization = 1e-10;
+    o->panel_width = 32;
+    o->precision = UCHOL_PRECISION_FP64;
+    o->block_width = 0;
+}
+
+int uchol_symbolic_create(const uchol_symbolic_desc* d, uchol_symbolic* out) {
+    return guarded([&] {
+        if (!d || !out) throw Error(UCHOL_BAD_ARG, "null argument");
+        *out = nullptr;
+        const int n = d->n, nnz = d->nnz, count = d->supernode_count;
+        if (n < 0 || nnz < 0 || count < 0) throw Error(UCHOL_BAD_ARG, "negative size");
+        if (n > 0 && (!d->row_ptr || !d->col || !d->permutation || !d->diag_value_index || !d->pattern_ptr ||
+                      !d->lower_start || !d->lower_value_ptr || !d->first_column || !d->parent || !d->child_ptr ||
+                      !d->front_ptr))
+            throw Error(UCHOL_BAD_ARG, "null symbolic array");
+        if ((n == 0) != (count == 0)) throw Error(UCHOL_BAD_ARG, "supernode count inconsistent with the size");
+        auto S = std::make_unique<uchol_symbolic_s>();
+        CK(cudaGetDevice(&S->device));
+        CK(cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking));
+        S->own_stream = true;
+        S->n = n;
+        S->nnz = nnz;
+        S->count = count;
+        auto cp = [](const int* p, long long len) { return p ? std::vector<int>(p, p + len) : std::vector<int>(); };
+        if (n > 0) {
+            S->row_ptr = cp(d->row_ptr, n + 1);
+            if (S->row_ptr[0] != 0 || S->row_ptr[n] != nnz) throw Error(UCHOL_BAD_ARG, "row pointers do not match nnz");
+            S->col = cp(d->col, nnz);
+            for (int r = 0; r < n; ++r) {
+                if (S->row_ptr[r + 1] < S->row_ptr[r]) throw Error(UCHOL_BAD_ARG, "row pointers are not monotone");
+                for (int k = S->row_ptr[r]; k < S->row_ptr[r + 1]; ++k)
+                    if (S->col[k] < r || S->col[k] >= n) throw Error(UCHOL_BAD_ARG, "column index outside the upper triangle");
+            }
+            S->perm = cp(d->permutation, n);
+            {
+                std::vector<char> seen(n, 0);
+                for (int v : S->perm) {
+                    if (v < 0 || v >= n || seen[v]) throw Error(UCHOL_BAD_ARG, "permutation is not a permutation");
+                    seen[v] = 1;
+                }
+            }
+            S->diag_idx = cp(d->diag_value_index, n);
+            for (int v : S->diag_idx)
+                if (v < -1 || v >= nnz) throw Error(UCHOL_BAD_ARG, "diagonal value index out of range");
+            S->pat_ptr = cp(d->pattern_ptr, n + 1);
+            if (S->pat_ptr[0] != 0) throw Error(UCHOL_BAD_ARG, "pattern pointers must start at 0");
+            for (int j = 0; j < n; ++j)
+                if (S->pat_ptr[j + 1] < S->pat_ptr[j]) throw Error(UCHOL_BAD_ARG, "pattern pointers are not monotone");
+            S->pat_rows = cp(d->pattern_rows, S->pat_ptr[n]);
+            S->lower_start = cp(d->lower_start, n);
+            S->lower_ptr = cp(d->lower_value_ptr, n + 1);
+            if (S->lower_ptr[0] != 0) throw Error(UCHOL_BAD_ARG, "lower pointers must start at 0");
+            for (int j = 0; j < n; ++j) {
+                if (S->lower_ptr[j + 1] < S->lower_ptr[j]) throw Error(UCHOL_BAD_ARG, "lower pointers are not monotone");
+                int len = S->lower_ptr[j + 1] - S->lower_ptr[j];
+                if (S->lower_start[j] != S->pat_ptr[j + 1] - len || S->lower_start[j] < S->pat_ptr[j])
+                    throw Error(UCHOL_BAD_ARG, "lower start inconsistent with the pattern");
+            }
+            S->lower_idx = cp(d->lower_value_index, S->lower_ptr[n]);
+            S->first_col = cp(d->first_column, count + 1);
+            S->parent = cp(d->parent, count);
+            S->child_ptr = cp(d->child_ptr, count + 1);
+            if (S->child_ptr[0] != 0 || S->child_ptr[count] < 0) throw Error(UCHOL_BAD_ARG, "child pointers invalid");
+            S->children = cp(d->children, S->child_ptr[count]);
+            S->front_ptr = cp(d->front_ptr, count + 1);
+            if (S->front_ptr[count] < 0) throw Error(UCHOL_BAD_ARG, "front pointers invalid");
+            for (int s = 0; s < count; ++s)
+                if (S->front_ptr[s + 1] < S->front_ptr[s]) throw Error(UCHOL_BAD_ARG, "front pointers are not monotone");
+            S->front_rows = cp(d->front_rows, S->front_ptr[count]);
+            // validates the whole structure (throws on any inconsistency)
+            PlanConfig probe;
+            try {
+                (void)build_plan(n, count, S->first_col.data(), S->parent.data(), S->child_ptr.data(),
+                                 S->children.data(), S->front_ptr.data(), S->front_rows.data(), S->diag_idx.data(),
+                                 S->pat_ptr.data(), S->pat_rows.data(), S->lower_start.data(), S->lower_ptr.data(),
+                                 S->lower_idx.data(), nnz, probe);
+            } catch (const std::runtime_error& e) {
+                throw Error(UCHOL_BAD_ARG, std::string("inconsistent symbolic factorization: ") + e.what());
+            }
+            S->d_perm.upload(S->perm, S->stream, "permutation");
+            S->d_diag_idx.upload(S->diag_idx, S->stream, "diagonal indices");
+            S->d_rows.upload(S->front_rows, S->stream, "front rows");
+            S->d_child_ptr.upload(S->child_ptr, S->stream, "children");
+            S->d_children.upload(S->children, S->stream, "children");
+            build_full_csr(S.get());
+            CK(cudaStreamSynchronize(S->stream));
+        }
+        *out = S.release();
+    });
+}
+
+int uchol_symbolic_destroy(uchol_symbolic s) {
+    return guarded([&] {
+        if (!s) return;
+        if (s->stream) cudaStreamSynchronize(s->stream);
+        cudaStream_t st = s->stream;
+        bool own = s->own_stream;
+        delete s;
+        if (own && st) cudaStreamDestroy(st);
+    });
+}
+
+int uchol_symbolic_set_stream(uchol_symbolic s, void* stream) {
+    return guarded([&] {
+        if (!s) throw Error(UCHOL_BAD_ARG, "null handle");
+        CK(cudaStreamSynchronize(s->stream));
+        if (s->own_stream) CK(cudaStreamDestroy(s->stream));
+        if (stream) {
+            s->stream = (cudaStream_t)stream;
+            s->own_stream = false;
+        } else {
+            CK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+            s->own_stream = true;
+        }
+    });
+}
+
+static int factorize_common(uchol_symbolic s, int n, int nnz, const double* values, bool on_device,
+                            const uchol_options* opts, uchol_factor* out, uchol_factor_stats* stats) {
+    return guarded([&] {
+        if (!out) throw Error(UCHOL_BAD_ARG, "null output handle");
+        *out = nullptr;
+        if (!s) throw Error(UCHOL_BAD_ARG, "symbolic handle is null");
+        if (!values && nnz > 0) throw Error(UCHOL_BAD_ARG, "values is null");
+        std::lock_guard<std::mutex> lk(s->mu);
+        std::unique_ptr<uchol_factor_s> F(create_factor(s, n, nnz, opts));
+        factorize_impl(F.get(), values, on_device);
+        if (stats) *stats = F->last;
+        *out = F.release();
+    });
+}
+
+int uchol_factorize(uchol_symbolic s, int n, int nnz, const double* values, const uchol_options* opts,
+                    uchol_factor* out, uchol_factor_stats* stats) {
+    return factorize_common(s, n, nnz, values, false, opts, out, stats);
+}
+
+int uchol_factorize_device(uchol_symbolic s, int n, int nnz, const double* d_values, const uchol_options* opts,
+                           uchol_factor* out, uchol_factor_stats* stats) {
+    return factorize_common(s, n, nnz, d_values, true, opts, out, stats);
+}
+
+int uchol_refactorize(uchol_factor f, const double* values, int on_device, uchol_factor_stats* stats) {
+    return guarded([&] {
+        if (!f || (!values && f->sym->nnz > 0)) throw Error(UCHOL_BAD_ARG, "null argument");
+        std::lock_guard<std::mutex> lk(f->mu);
+        factorize_impl(f, values, on_device != 0);
+        if (stats) *stats = f->last;
+    });
+}
+
+int uchol_factor_destroy(uchol_factor f) {
+    return guarded([&] {
+        if (!f) return;
+        cudaStreamSynchronize(f->sym->stream);
+        destroy_tc_maps(f->maps);
+        delete f;
+    });
+}
+
+int uchol_factor_diagonal(uchol_factor f, double* out) {
+    return guarded([&] {
+        if (!f || (!out && f->sym->n > 0)) throw Error(UCHOL_BAD_ARG, "null argument");
+        if (f->sym->n == 0) return;
+        CK(cudaMemcpyAsync(out, f->diag.p, (size_t)f->sym->n * sizeof(double), cudaMemcpyDeviceToHost, f->sym->stream));
+        CK(cudaStreamSynchronize(f->sym->stream));
+    });
+}
+
+int uchol_factor_get_stats(uchol_factor f, uchol_factor_stats* stats) {
+    return guarded([&] {
+        if (!f || !stats) throw Error(UCHOL_BAD_ARG, "null argument");
+        *stats = f->last;
+    });
+}
+
+int uchol_factor_phase_times(uchol_factor f, uchol_phase_times* t) {
+    return guarded([&] {
+        if (!f || !t) throw Error(UCHOL_BAD_ARG, "null argument");
+        *t = f->phases;
+    });
+}
+
+static void check_solve_args(uchol_factor f, int n, int nrhs, const void* b, int ldb, const void* x, int ldx) {
+    if (!f) throw Error(UCHOL_BAD_ARG, "factor handle is null");
+    if (n != f->sym->n)
+        throw Error(UCHOL_BAD_ARG, "The right-hand side length " + std::to_string(n) +
+                                       " does not match the matrix size " + std::to_string(f->sym->n) + ".");
+    if (nrhs < 0 || nrhs > 65535) throw Error(UCHOL_BAD_ARG, "invalid number of right-hand sides");
+    if (n > 0 && nrhs > 0 && (!b || !x)) throw Error(UCHOL_BAD_ARG, "null vector");
+    if (ldb < std::max(1, n) || ldx < std::max(1, n)) throw Error(UCHOL_BAD_ARG, "leading dimension smaller than n");
+}
+
+int uchol_solve_device(uchol_factor f, int n, int nrhs, const double* b, int ldb, double* x, int ldx) {
+    return guarded([&] {
+        check_solve_args(f, n, nrhs, b, ldb, x, ldx);
+        if (n == 0 || nrhs == 0) return;
+        std::lock_guard<std::mutex> lk(f->mu);
+        ensure_workspace(f, nrhs);
+        apply_factor(f, nrhs, b, ldb, x, ldx);
+        CK(cudaStreamSynchronize(f->sym->stream));
+    });
+}
+
+int uchol_solve(uchol_factor f, int n, int nrhs, const double* b, int ldb, double* x, int ldx) {
+    return guarded([&] {
+        check_solve_args(f, n, nrhs, b, ldb, x, ldx);
+        if (n == 0 || nrhs == 0) return;
+        std::lock_guard<std::mutex> lk(f->mu);
+        cudaStream_t st = f->sym->stream;
+        ensure_workspace(f, nrhs);
+        double* db = f->vec[4].as<double>();
+        double* dx = f->vec[5].as<double>();
+        CK(cudaMemcpy2DAsync(db, (size_t)n * 8, b, (size_t)ldb * 8, (size_t)n * 8, nrhs, cudaMemcpyHostToDevice, st));
+        apply_factor(f, nrhs, db, n, dx, n);
+        CK(cudaMemcpy2DAsync(x, (size_t)ldx * 8, dx, (size_t)n * 8, (size_t)n * 8, nrhs, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+    });
+}
+
+int uchol_solve_refined_device(uchol_factor f, int n, int nrhs, const double* b, int ldb, double* x, int ldx,
+                               const uchol_refine_options* ro, uchol_refine_stats* rs) {
+    return guarded([&] {
+        check_solve_args(f, n, nrhs, b, ldb, x, ldx);
+        if (rs) *rs = {0, 0.0, 0.0, 0.0};
+        if (n == 0 || nrhs == 0) return;
+        std::lock_guard<std::mutex> lk(f->mu);
+        solve_refined(f, nrhs, b, ldb, x, ldx, ro, rs);
+    });
+}
+
+int uchol_solve_refined(uchol_factor f, int n, int nrhs, const double* b, int ldb, double* x, int ldx,
+                        const uchol_refine_options* ro, uchol_refine_stats* rs) {
+    return guarded([&] {
+        check_solve_args(f, n, nrhs, b, ldb, x, ldx);
+        if (rs) *rs = {0, 0.0, 0.0, 0.0};
+        if (n == 0 || nrhs == 0) return;
+        std::lock_guard<std::mutex> lk(f->mu);
+        cudaStream_t st = f->sym->stream;
+        ensure_workspace(f, nrhs);
+        DBuf db, dx;
+        db.alloc((size_t)n * nrhs * 8, "right-hand sides");
+        dx.alloc((size_t)n * nrhs * 8, "solutions");
+        CK(cudaMemcpy2DAsync(db.p, (size_t)n * 8, b, (size_t)ldb * 8, (size_t)n * 8, nrhs, cudaMemcpyHostToDevice, st));
+        int code = UCHOL_OK;
+        std::string msg;
+        try {
+            solve_refined(f, nrhs, db.as<double>(), n, dx.as<double>(), n, ro, rs);
+        } catch (const Error& e) {
+            if (e.code != UCHOL_NO_CONVERGENCE) throw;
+            code = e.code;
+            msg = e.what();
+        }
+        CK(cudaMemcpy2DAsync(x, (size_t)ldx * 8, dx.p, (size_t)n * 8, (size_t)n * 8, nrhs, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        if (code != UCHOL_OK) throw Error(code, msg);
+    });
+}
+
+int uchol_residual_norms(uchol_factor f, int n, int nrhs, const double* b, int ldb, const double* x, int ldx,
+                         double* out) {
+    return guarded([&] {
+        check_solve_args(f, n, nrhs, b, ldb, x, ldx);
+        if (!out && nrhs > 0) throw Error(UCHOL_BAD_ARG, "null output");
+        if (nrhs == 0) return;
+        if (n == 0) {
+            for (int j = 0; j < nrhs; ++j) out[j] = 0.0;
+            return;
+        }
+        std::lock_guard<std::mutex> lk(f->mu);
+        cudaStream_t st = f->sym->stream;
+        ensure_workspace(f, nrhs);
+        double* db = f->vec[4].as<double>();
+        double* dx = f->vec[5].as<double>();
+        double* r = f->vec[0].as<double>();
+        CK(cudaMemcpy2DAsync(db, (size_t)n * 8, b, (size_t)ldb * 8, (size_t)n * 8, nrhs, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpy2DAsync(dx, (size_t)n * 8, x, (size_t)ldx * 8, (size_t)n * 8, nrhs, cudaMemcpyHostToDevice, st));
+        residual(f, nrhs, dx, n, db, n, r, n);
+        double* nr = f->scal.as<double>() + kDotBlocks * nrhs;
+        dots(f, nrhs, r, n, r, n, nr);
+        std::vector<double> h(nrhs);
+        CK(cudaMemcpyAsync(h.data(), nr, nrhs * sizeof(double), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        for (int j = 0; j < nrhs; ++j) out[j] = std::sqrt(h[j]);
+    });
+}
+
+}  // extern "C"

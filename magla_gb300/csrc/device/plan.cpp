@@ -1,0 +1,433 @@
+// Execution plan of the device numeric phase (see plan.hpp).
+#include "plan.hpp"
+
+#include <algorithm>
+#include <map>
+#include <stdexcept>
+
+namespace uchol_dev {
+
+namespace {
+
+inline long long round_up(long long x, long long a) { return (x + a - 1) / a * a; }
+
+void fail(const std::string& m) { throw std::runtime_error(m); }
+
+// First-fit allocator over one arena, used to plan the lifetimes of the
+// contribution blocks ahead of time (no device allocation at run time).
+class ArenaPlanner {
+public:
+    long long alloc(long long size) {
+        for (auto it = free_.begin(); it != free_.end(); ++it) {
+            if (it->second >= size) {
+                long long off = it->first;
+                long long rest = it->second - size;
+                free_.erase(it);
+                if (rest > 0) free_[off + size] = rest;
+                return off;
+            }
+        }
+        long long off = top_;
+        // extend the last free block if it touches the top
+        if (!free_.empty()) {
+            auto last = std::prev(free_.end());
+            if (last->first + last->second == top_) {
+                off = last->first;
+                free_.erase(last);
+            }
+        }
+        top_ = off + size;
+        peak_ = std::max(peak_, top_);
+        return off;
+    }
+    void release(long long off, long long size) {
+        auto it = free_.emplace(off, size).first;
+        auto next = std::next(it);
+        if (next != free_.end() && it->first + it->second == next->first) {
+            it->second += next->second;
+            free_.erase(next);
+        }
+        if (it != free_.begin()) {
+            auto prev = std::prev(it);
+            if (prev->first + prev->second == it->first) {
+                prev->second += it->second;
+                free_.erase(it);
+                it = prev;
+            }
+        }
+        if (it->first + it->second == top_) {
+            top_ = it->first;
+            free_.erase(it);
+        }
+    }
+    long long peak() const { return peak_; }
+
+private:
+    std::map<long long, long long> free_;
+    long long top_ = 0, peak_ = 0;
+};
+
+}  // namespace
+
+Plan build_plan(int n, int count, const int* first_column, const int* parent, const int* child_ptr,
+                const int* children, const int* front_ptr, const int* front_rows, const int* diag_value_index,
+                const int* pattern_ptr, const int* pattern_rows, const int* lower_start, const int* lower_value_ptr,
+                const int* lower_value_index, int nnz, const PlanConfig& cfg) {
+    Plan P;
+    P.cfg = cfg;
+    P.n = n;
+    P.count = count;
+    if (count == 0) return P;
+
+    // ---- validation of the symbolic input (every device index is checked here) ----
+    if (first_column[0] != 0 || first_column[count] != n) fail("first_column does not span 0..n");
+    if (front_ptr[0] != 0) fail("front_ptr must start at 0");
+    for (int s = 0; s < count; ++s) {
+        int w = first_column[s + 1] - first_column[s];
+        int m = front_ptr[s + 1] - front_ptr[s];
+        if (w < 1 || m < w) fail("supernode " + std::to_string(s) + " has an invalid width or front size");
+        if (parent[s] != -1 && (parent[s] <= s || parent[s] >= count)) fail("supernode parents must follow their children");
+        const int* rows = front_rows + front_ptr[s];
+        for (int a = 0; a < m; ++a) {
+            if (rows[a] < 0 || rows[a] >= n) fail("front row index out of range");
+            if (a > 0 && rows[a] <= rows[a - 1]) fail("front rows are not strictly ascending");
+            if (a < w && rows[a] != first_column[s] + a) fail("front rows must start with the supernode's columns");
+        }
+        if (m > w && parent[s] < 0) fail("a root supernode cannot have trailing rows");
+        if (child_ptr[s + 1] < child_ptr[s]) fail("child pointers are not monotone");
+        for (int c = child_ptr[s]; c < child_ptr[s + 1]; ++c)
+            if (children[c] < 0 || children[c] >= s || parent[children[c]] != s) fail("children list inconsistent with parents");
+    }
+    if ((long long)pattern_ptr[n] < 0 || lower_value_ptr[n] < 0) fail("negative pattern length");
+
+    // ---- levels (height in the assembly tree) ----
+    P.level_of.assign(count, 0);
+    for (int s = 0; s < count; ++s)
+        if (parent[s] >= 0) P.level_of[parent[s]] = std::max(P.level_of[parent[s]], P.level_of[s] + 1);
+    P.levels = 0;
+    for (int s = 0; s < count; ++s) P.levels = std::max(P.levels, P.level_of[s] + 1);
+    std::vector<std::vector<int>> at_level(P.levels);
+    for (int s = 0; s < count; ++s) at_level[P.level_of[s]].push_back(s);
+
+    // ---- per-supernode geometry, relative indices ----
+    P.sn.resize(count);
+    long long rel_total = 0;
+    for (int s = 0; s < count; ++s) {
+        SnDev& d = P.sn[s];
+        d.w = first_column[s + 1] - first_column[s];
+        d.m = front_ptr[s + 1] - front_ptr[s];
+        d.first_col = first_column[s];
+        d.rows_off = front_ptr[s];
+        d.parent = parent[s];
+        d.ldp = (int)round_up(d.m, 8);
+        int t = d.m - d.w;
+        d.ldc = t > 0 ? (int)round_up(t, 8) : 0;
+        d.rel_off = (int)rel_total;
+        rel_total += t;
+    }
+    if (rel_total > INT32_MAX) fail("too many trailing rows for 32-bit offsets");
+    P.rel.assign(rel_total, 0);
+    for (int s = 0; s < count; ++s) {
+        const SnDev& d = P.sn[s];
+        int t = d.m - d.w;
+        if (t == 0) continue;
+        const SnDev& pd = P.sn[parent[s]];
+        const int* prow = front_rows + front_ptr[parent[s]];
+        const int* crow = front_rows + front_ptr[s] + d.w;
+        int q = 0;
+        for (int a = 0; a < t; ++a) {
+            while (q < pd.m && prow[q] < crow[a]) ++q;
+            if (q == pd.m || prow[q] != crow[a])
+                fail("trailing row of supernode " + std::to_string(s) + " is missing from its parent's pattern");
+            P.rel[d.rel_off + a] = q;
+        }
+    }
+
+    // ---- factor panels (persistent) ----
+    long long off = 0;
+    for (int s = 0; s < count; ++s) {
+        SnDev& d = P.sn[s];
+        d.panel_off = off;
+        off += round_up((long long)d.ldp * d.w, 64);
+    }
+    P.factor_elems = off;
+
+    // ---- contribution blocks: lifetime [level(s), level(parent)] ----
+    {
+        ArenaPlanner arena;
+        std::vector<long long> size(count, 0);
+        for (int L = 0; L < P.levels; ++L) {
+            for (int s : at_level[L]) {
+                SnDev& d = P.sn[s];
+                int t = d.m - d.w;
+                if (t == 0) {
+                    d.contrib_off = -1;
+                    continue;
+                }
+                size[s] = round_up((long long)d.ldc * t, 64);
+                d.contrib_off = arena.alloc(size[s]);
+            }
+            for (int s : at_level[L])
+                for (int c = child_ptr[s]; c < child_ptr[s + 1]; ++c) {
+                    int ch = children[c];
+                    if (size[ch] > 0) arena.release(P.sn[ch].contrib_off, size[ch]);
+                }
+        }
+        P.contrib_elems = std::max<long long>(arena.peak(), 64);
+    }
+
+    // ---- assembly map ----
+    P.assemble_pos.assign(nnz, -1);
+    {
+        std::vector<int> row_map(n, -1);
+        for (int s = 0; s < count; ++s) {
+            const SnDev& d = P.sn[s];
+            const int* rows = front_rows + front_ptr[s];
+            for (int a = 0; a < d.m; ++a) row_map[rows[a]] = a;
+            for (int lc = 0; lc < d.w; ++lc) {
+                int j = d.first_col + lc;
+                int di = diag_value_index[j];
+                if (di >= 0) {
+                    if (di >= nnz || P.assemble_pos[di] != -1) fail("diagonal value index invalid or repeated");
+                    P.assemble_pos[di] = d.panel_off + lc + (long long)lc * d.ldp;
+                }
+                int lb = lower_value_ptr[j];
+                for (int p = lower_start[j]; p < pattern_ptr[j + 1]; ++p) {
+                    int r = pattern_rows[p];
+                    if (r <= j || r >= n) fail("lower pattern row out of range");
+                    int lr = row_map[r];
+                    if (lr < 0 || rows[lr] != r) fail("matrix entry outside the supernode's row pattern");
+                    int vi = lower_value_index[lb + (p - lower_start[j])];
+                    if (vi < 0 || vi >= nnz || P.assemble_pos[vi] != -1) fail("lower value index invalid or repeated");
+                    P.assemble_pos[vi] = d.panel_off + lr + (long long)lc * d.ldp;
+                }
+            }
+            for (int a = 0; a < d.m; ++a) row_map[rows[a]] = -1;
+        }
+        for (int k = 0; k < nnz; ++k)
+            if (P.assemble_pos[k] < 0) fail("a matrix value is not referenced by the symbolic pattern");
+    }
+
+    // ---- factorisation launches, level by level ----
+    const int PB = cfg.pivot_block;
+    const int NB = cfg.tensor_core ? cfg.outer_block : cfg.pivot_block;
+    const int TS = cfg.tile;
+    for (int L = 0; L < P.levels; ++L) {
+        const auto& fronts = at_level[L];
+        // clear contribution blocks of this level
+        int zb = (int)P.zero_off.size();
+        for (int s : fronts) {
+            const SnDev& d = P.sn[s];
+            if (d.m > d.w) {
+                P.zero_off.push_back(d.contrib_off);
+                P.zero_len.push_back((long long)d.ldc * (d.m - d.w));
+            }
+        }
+        if ((int)P.zero_off.size() > zb) P.launches.push_back({Launch::ZeroContrib, zb, (int)P.zero_off.size() - zb, 0});
+
+        // extend-add: one item per receiving parent column
+        int ib = (int)P.ea_items.size();
+        for (int s : fronts) {
+            struct Rec { int pcol, order, child, a; };
+            std::vector<Rec> recs;
+            for (int c = child_ptr[s]; c < child_ptr[s + 1]; ++c) {
+                int ch = children[c];
+                const SnDev& cd = P.sn[ch];
+                int t = cd.m - cd.w;
+                for (int a = 0; a < t; ++a) recs.push_back({P.rel[cd.rel_off + a], c, ch, a});
+            }
+            std::stable_sort(recs.begin(), recs.end(), [](const Rec& x, const Rec& y) {
+                return x.pcol != y.pcol ? x.pcol < y.pcol : x.order < y.order;
+            });
+            size_t q = 0;
+            while (q < recs.size()) {
+                EaItem it;
+                it.parent = s;
+                it.pcol = recs[q].pcol;
+                it.begin = (int)P.ea_entries.size();
+                for (; q < recs.size() && recs[q].pcol == it.pcol; ++q) P.ea_entries.push_back({recs[q].child, recs[q].a});
+                it.end = (int)P.ea_entries.size();
+                P.ea_items.push_back(it);
+            }
+        }
+        if ((int)P.ea_items.size() > ib) P.launches.push_back({Launch::ExtendAdd, ib, (int)P.ea_items.size() - ib, 0});
+
+        // small fronts: one CTA each
+        int sb = (int)P.small_fronts.size();
+        std::vector<int> large;
+        for (int s : fronts) {
+            if (P.sn[s].m <= cfg.small_max) {
+                P.small_fronts.push_back(s);
+                P.max_small_m = std::max(P.max_small_m, P.sn[s].m);
+            } else {
+                large.push_back(s);
+            }
+        }
+        if ((int)P.small_fronts.size() > sb) P.launches.push_back({Launch::SmallFronts, sb, (int)P.small_fronts.size() - sb, 0});
+
+        // large fronts: blocked right-looking factorisation in lockstep
+        int max_w = 0;
+        for (int s : large) max_w = std::max(max_w, P.sn[s].w);
+        for (int k0 = 0; k0 < max_w; k0 += NB) {
+            // staging rows of this outer step (tensor-core operands of the trailing update)
+            std::map<int, long long> stage_base;
+            long long stage_top = 0;
+            if (cfg.tensor_core) {
+                for (int s : large) {
+                    const SnDev& d = P.sn[s];
+                    if (d.w <= k0) continue;
+                    int nbo = std::min(NB, d.w - k0);
+                    int rows = d.m - (k0 + nbo);
+                    if (rows > 0) {
+                        stage_base[s] = stage_top;
+                        stage_top += round_up(rows, 128);
+                    }
+                }
+                P.stage_rows = std::max(P.stage_rows, stage_top);
+            }
+            for (int j0r = 0; j0r < NB; j0r += PB) {
+                int qb = (int)P.pivot_tasks.size();
+                int pb = (int)P.panel_tasks.size();
+                int ub = (int)P.simt_tasks.size();
+                for (int s : large) {
+                    const SnDev& d = P.sn[s];
+                    if (d.w <= k0) continue;
+                    int nbo = std::min(NB, d.w - k0);
+                    int j0 = k0 + j0r;
+                    if (j0r >= nbo) continue;
+                    int nbi = std::min(PB, k0 + nbo - j0);
+                    int outer_end = k0 + nbo;
+                    P.pivot_tasks.push_back({s, j0, nbi, j0 + nbi, 0, -1, 0, 0});
+                    // TRSM tasks over rows [j0+nbi, m), broken at outer_end for staging
+                    int r = j0 + nbi;
+                    while (r < d.m) {
+                        int lim = r < outer_end ? outer_end : d.m;
+                        int rows = std::min(128, lim - r);
+                        int srow = -1, zero_to = 0;
+                        if (cfg.tensor_core && r >= outer_end) {
+                            srow = (int)(stage_base[s] + (r - outer_end));
+                            if (j0 + nbi == outer_end && nbo < NB) zero_to = NB;
+                        }
+                        P.panel_tasks.push_back({s, j0, nbi, r, rows, srow, j0 - k0, zero_to});
+                        r += rows;
+                    }
+                    // inner update of the rest of the outer block (tensor-core configuration only)
+                    if (NB != PB && j0 + nbi < outer_end) {
+                        for (int jc = j0 + nbi; jc < outer_end; jc += TS) {
+                            int jend = std::min(jc + TS, outer_end);
+                            for (int i0 = jc; i0 < d.m; i0 += TS)
+                                P.simt_tasks.push_back({s, i0, jc, j0, nbi, -1, -1, jend});
+                        }
+                    }
+                }
+                if ((int)P.pivot_tasks.size() > qb) P.launches.push_back({Launch::PivotBlock, qb, (int)P.pivot_tasks.size() - qb, 0});
+                if ((int)P.panel_tasks.size() > pb) P.launches.push_back({Launch::Trsm, pb, (int)P.panel_tasks.size() - pb, 0});
+                if ((int)P.simt_tasks.size() > ub) P.launches.push_back({Launch::SimtUpdate, ub, (int)P.simt_tasks.size() - ub, 0});
+                if (!cfg.tensor_core) break;  // FP64 path: one pivot block per outer step
+            }
+            // trailing update of the outer step
+            int tb = cfg.tensor_core ? (int)P.tc_tasks.size() : (int)P.simt_tasks.size();
+            for (int s : large) {
+                const SnDev& d = P.sn[s];
+                if (d.w <= k0) continue;
+                int nbo = std::min(NB, d.w - k0);
+                int c0 = k0 + nbo;
+                if (c0 >= d.m) continue;
+                int tn = cfg.tensor_core ? cfg.tc_tile_n : TS;
+                int tm = cfg.tensor_core ? cfg.tc_tile_m : TS;
+                for (int jc = c0; jc < d.m;) {
+                    int split = jc < d.w ? d.w : d.m;   // tiles never straddle the panel/contrib split
+                    int jend = std::min(jc + tn, split);
+                    for (int i0 = jc; i0 < d.m; i0 += tm) {
+                        if (cfg.tensor_core) {
+                            int ar = (int)(stage_base[s] + (i0 - c0));
+                            int br = (int)(stage_base[s] + (jc - c0));
+                            P.tc_tasks.push_back({s, i0, jc, k0, nbo, ar, br, jend});
+                        } else {
+                            P.simt_tasks.push_back({s, i0, jc, k0, nbo, -1, -1, jend});
+                        }
+                    }
+                    jc = jend;
+                }
+            }
+            if (cfg.tensor_core) {
+                if ((int)P.tc_tasks.size() > tb) P.launches.push_back({Launch::TcUpdate, tb, (int)P.tc_tasks.size() - tb, 0});
+            } else {
+                if ((int)P.simt_tasks.size() > tb) P.launches.push_back({Launch::SimtUpdate, tb, (int)P.simt_tasks.size() - tb, 0});
+            }
+        }
+    }
+
+    // ---- solves ----
+    P.fvec_off.assign(count, 0);
+    long long fo = 0;
+    for (int s = 0; s < count; ++s) {
+        P.fvec_off[s] = fo;
+        fo += round_up(P.sn[s].m, 8);
+    }
+    P.fvec_elems = std::max<long long>(fo, 8);
+    const int SB = cfg.solve_block;
+    for (int L = 0; L < P.levels; ++L) {
+        const auto& fronts = at_level[L];
+        int fb = (int)P.solve_fronts.size();
+        P.solve_fronts.insert(P.solve_fronts.end(), fronts.begin(), fronts.end());
+        int fcount = (int)fronts.size();
+        P.fwd_launches.push_back({SolveLaunch::FwdGather, fb, fcount});
+        int max_w = 0;
+        for (int s : fronts) max_w = std::max(max_w, P.sn[s].w);
+        for (int k0 = 0; k0 < max_w; k0 += SB) {
+            int db = (int)P.solve_tasks.size();
+            for (int s : fronts)
+                if (P.sn[s].w > k0) P.solve_tasks.push_back({s, k0, std::min(SB, P.sn[s].w - k0), 0, 0});
+            P.fwd_launches.push_back({SolveLaunch::FwdDiag, db, (int)P.solve_tasks.size() - db});
+            int rb = (int)P.solve_tasks.size();
+            for (int s : fronts) {
+                const SnDev& d = P.sn[s];
+                if (d.w <= k0) continue;
+                int kn = std::min(SB, d.w - k0);
+                for (int r = k0 + kn; r < d.m; r += 128)
+                    P.solve_tasks.push_back({s, k0, kn, r, std::min(d.m, r + 128)});
+            }
+            if ((int)P.solve_tasks.size() > rb) P.fwd_launches.push_back({SolveLaunch::FwdRows, rb, (int)P.solve_tasks.size() - rb});
+        }
+        P.fwd_launches.push_back({SolveLaunch::FwdFinish, fb, fcount});
+    }
+    for (int L = P.levels - 1; L >= 0; --L) {
+        const auto& fronts = at_level[L];
+        // fronts of this level are already listed contiguously in solve_fronts; find them
+        int fb = 0;
+        for (int l = 0; l < L; ++l) fb += (int)at_level[l].size();
+        int fcount = (int)fronts.size();
+        P.bwd_launches.push_back({SolveLaunch::BwdGather, fb, fcount});
+        int tb = (int)P.solve_tasks.size();
+        for (int s : fronts) {
+            const SnDev& d = P.sn[s];
+            if (d.m == d.w) continue;
+            for (int c = 0; c < d.w; c += 8) P.solve_tasks.push_back({s, c, std::min(8, d.w - c), d.w, d.m});
+        }
+        if ((int)P.solve_tasks.size() > tb) P.bwd_launches.push_back({SolveLaunch::BwdTail, tb, (int)P.solve_tasks.size() - tb});
+        int max_w = 0;
+        for (int s : fronts) max_w = std::max(max_w, P.sn[s].w);
+        int blocks = (max_w + SB - 1) / SB;
+        for (int b = blocks - 1; b >= 0; --b) {
+            int k0 = b * SB;
+            int db = (int)P.solve_tasks.size();
+            for (int s : fronts)
+                if (P.sn[s].w > k0) P.solve_tasks.push_back({s, k0, std::min(SB, P.sn[s].w - k0), 0, 0});
+            P.bwd_launches.push_back({SolveLaunch::BwdDiag, db, (int)P.solve_tasks.size() - db});
+            if (k0 == 0) continue;
+            int cb = (int)P.solve_tasks.size();
+            for (int s : fronts) {
+                const SnDev& d = P.sn[s];
+                if (d.w <= k0) continue;
+                int kn = std::min(SB, d.w - k0);
+                for (int c = 0; c < k0; c += 8) P.solve_tasks.push_back({s, c, std::min(8, k0 - c), k0, k0 + kn});
+            }
+            if ((int)P.solve_tasks.size() > cb) P.bwd_launches.push_back({SolveLaunch::BwdCols, cb, (int)P.solve_tasks.size() - cb});
+        }
+        P.bwd_launches.push_back({SolveLaunch::BwdFinish, fb, fcount});
+    }
+    return P;
+}
+
+}  // namespace uchol_dev

@@ -1,0 +1,83 @@
+// Host-side execution plan of the device numeric phase: tree levels, memory
+// layout of fronts, and the task lists every kernel launch consumes.  Built
+// once per (symbolic pattern, block configuration) and reused by every
+// factorisation and solve.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+
+namespace uchol_dev {
+
+struct PlanConfig {
+    int pivot_block = 32;     // FP64 pivot block (the reference's PanelWidth)
+    int outer_block = 32;     // Schur-update block (== pivot_block on the FP64 path)
+    int small_max = 96;       // fronts with m <= small_max are factorised by one CTA in shared memory
+    int tile = 64;            // SIMT tile edge (update kernels)
+    int tc_tile_m = 128;      // tensor-core tile
+    int tc_tile_n = 128;
+    bool tensor_core = false; // outer updates on tcgen05 from staged operands
+    int solve_block = 64;     // column block of the triangular solves
+};
+
+// One kernel launch: a contiguous range of tasks in one of the task arrays.
+struct Launch {
+    enum Kind : int {
+        ZeroContrib, ExtendAdd, SmallFronts, PivotBlock, Trsm, SimtUpdate, TcUpdate
+    } kind;
+    int begin, count;   // task range
+    int aux;            // kind-specific (e.g. staging tensor-map index)
+};
+
+struct SolveLaunch {
+    enum Kind : int {
+        FwdGather, FwdDiag, FwdRows, FwdFinish, BwdGather, BwdTail, BwdDiag, BwdCols, BwdFinish
+    } kind;
+    int begin, count;
+};
+
+struct SolveBlockTask {   // block [k0, k0+kn) of supernode s; rows [r0, r1) for row/column updates
+    int s, k0, kn, r0, r1;
+};
+
+struct Plan {
+    PlanConfig cfg;
+    int n = 0, count = 0, levels = 0;
+    std::vector<int> level_of;                 // per supernode
+    std::vector<SnDev> sn;                     // per supernode
+    std::vector<int> rel;                      // parent-local index of each trailing row
+    std::vector<long long> assemble_pos;       // per matrix value: offset in the factor arena
+    long long factor_elems = 0;                // panels
+    long long contrib_elems = 0;               // contribution arena (planned peak)
+    long long fvec_elems = 0;                  // front-vector workspace of the solves (per RHS)
+    std::vector<long long> fvec_off;           // per supernode offset into the front-vector workspace
+
+    // factorisation tasks
+    std::vector<long long> zero_off, zero_len;   // contribution blocks cleared before extend-add
+    std::vector<EaItem> ea_items;
+    std::vector<EaEntry> ea_entries;
+    std::vector<int> small_fronts;
+    std::vector<PanelTask> pivot_tasks;   // one per (front, pivot block)
+    std::vector<PanelTask> panel_tasks;   // TRSM row chunks
+    std::vector<TileTask> simt_tasks;
+    std::vector<TileTask> tc_tasks;
+    std::vector<Launch> launches;
+    int max_small_m = 0;
+    long long stage_rows = 0;                  // rows of the operand staging arena (tensor-core path)
+
+    // solve tasks
+    std::vector<int> solve_fronts;             // supernode lists for gather/finish launches
+    std::vector<SolveBlockTask> solve_tasks;
+    std::vector<SolveLaunch> fwd_launches, bwd_launches;
+};
+
+// Throws std::runtime_error on inconsistent symbolic input.
+Plan build_plan(int n, int count, const int* first_column, const int* parent, const int* child_ptr,
+                const int* children, const int* front_ptr, const int* front_rows, const int* diag_value_index,
+                const int* pattern_ptr, const int* pattern_rows, const int* lower_start, const int* lower_value_ptr,
+                const int* lower_value_index, int nnz, const PlanConfig& cfg);
+
+}  // namespace uchol_dev

@@ -1,0 +1,276 @@
+// Supernodal triangular solves (multifrontal form), FP64 symmetric product
+// and vector kernels for refinement.
+//
+// Forward U^T y = b follows the multifrontal schedule: each supernode
+// gathers its right-hand side plus the update vectors of its children
+// (extend-add of vectors, child order, no atomics), solves with its
+// diagonal block and leaves the update vector of its trailing rows for the
+// parent.  Backward U x = z reads the final values of the trailing rows
+// (ancestors) directly.  The result equals the reference's supernodal
+// substitutions (CAESolvers/UCHOL/UtduNumericFactorization.cs:139-207);
+// only the order of the floating-point sums differs.
+#pragma once
+
+#include "common.cuh"
+#include "plan.hpp"
+
+namespace uchol_dev {
+
+struct SolveArgs {
+    const SnDev* sn;
+    const int* rel;
+    const int* rows;        // front_rows
+    const int* child_ptr;
+    const int* children;
+    const long long* fvec_off;
+    long long fv_stride;    // elements between RHS columns in the front-vector workspace
+    int n, nrhs, ldw;       // ldw: leading dimension of the work vector
+};
+
+template <class Cv>
+__global__ void k_permute_in(const double* __restrict__ b, int ldb, const int* __restrict__ perm, int n, int nrhs,
+                             Cv* __restrict__ work, int ldw) {
+    for (int r = blockIdx.y; r < nrhs; r += gridDim.y)
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+            work[i + (long long)r * ldw] = (Cv)b[perm[i] + (long long)r * ldb];
+}
+
+template <class Cv>
+__global__ void k_permute_out(const Cv* __restrict__ work, int ldw, const int* __restrict__ perm, int n, int nrhs,
+                              double* __restrict__ x, int ldx) {
+    for (int r = blockIdx.y; r < nrhs; r += gridDim.y)
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+            x[perm[i] + (long long)r * ldx] = (double)work[i + (long long)r * ldw];
+}
+
+template <class Cv>
+__global__ void k_fwd_gather(const int* __restrict__ fronts, SolveArgs A, const Cv* __restrict__ work,
+                             Cv* __restrict__ fv) {
+    const int s = fronts[blockIdx.x];
+    const SnDev d = A.sn[s];
+    for (int r = 0; r < A.nrhs; ++r) {
+        Cv* f = fv + A.fvec_off[s] + r * A.fv_stride;
+        for (int a = threadIdx.x; a < d.m; a += blockDim.x)
+            f[a] = a < d.w ? work[d.first_col + a + (long long)r * A.ldw] : Cv(0);
+        __syncthreads();
+        for (int c = A.child_ptr[s]; c < A.child_ptr[s + 1]; ++c) {
+            const int ch = A.children[c];
+            const SnDev cd = A.sn[ch];
+            const int t = cd.m - cd.w;
+            const Cv* u = fv + A.fvec_off[ch] + r * A.fv_stride + cd.w;
+            const int* rl = A.rel + cd.rel_off;
+            for (int b = threadIdx.x; b < t; b += blockDim.x) f[rl[b]] += u[b];
+            __syncthreads();
+        }
+    }
+}
+
+// Unit lower triangular solve with the diagonal block [k0, k0+kn).
+template <class T, class Cv>
+__global__ void k_fwd_diag(const SolveBlockTask* __restrict__ tasks, SolveArgs A, const T* __restrict__ panel,
+                           Cv* __restrict__ fv) {
+    __shared__ Cv Lb[64 * 65];
+    __shared__ Cv x[64];
+    const SolveBlockTask tk = tasks[blockIdx.x];
+    const SnDev d = A.sn[tk.s];
+    const T* P = panel + d.panel_off;
+    const int kn = tk.kn;
+    for (int idx = threadIdx.x; idx < kn * kn; idx += blockDim.x) {
+        int r = idx % kn, c = idx / kn;
+        Lb[r + c * 65] = r > c ? (Cv)P[(tk.k0 + r) + (long long)(tk.k0 + c) * d.ldp] : Cv(0);
+    }
+    for (int r = 0; r < A.nrhs; ++r) {
+        Cv* f = fv + A.fvec_off[tk.s] + r * A.fv_stride + tk.k0;
+        __syncthreads();
+        if (threadIdx.x < kn) x[threadIdx.x] = f[threadIdx.x];
+        __syncthreads();
+        for (int k = 0; k < kn - 1; ++k) {
+            const Cv xk = x[k];
+            __syncthreads();
+            int i = threadIdx.x;
+            if (i > k && i < kn) x[i] -= Lb[i + k * 65] * xk;
+            __syncthreads();
+        }
+        if (threadIdx.x < kn) f[threadIdx.x] = x[threadIdx.x];
+    }
+}
+
+// f[i] -= sum_{k in block} L[i,k] f[k] for rows [r0, r1).
+template <class T, class Cv>
+__global__ void k_fwd_rows(const SolveBlockTask* __restrict__ tasks, SolveArgs A, const T* __restrict__ panel,
+                           Cv* __restrict__ fv) {
+    __shared__ Cv xb[64];
+    const SolveBlockTask tk = tasks[blockIdx.x];
+    const SnDev d = A.sn[tk.s];
+    const T* P = panel + d.panel_off;
+    const int i = tk.r0 + threadIdx.x;
+    for (int r = 0; r < A.nrhs; ++r) {
+        Cv* f = fv + A.fvec_off[tk.s] + r * A.fv_stride;
+        __syncthreads();
+        if (threadIdx.x < tk.kn) xb[threadIdx.x] = f[tk.k0 + threadIdx.x];
+        __syncthreads();
+        if (i < tk.r1) {
+            Cv acc = Cv(0);
+            for (int k = 0; k < tk.kn; ++k) acc += (Cv)P[i + (long long)(tk.k0 + k) * d.ldp] * xb[k];
+            f[i] -= acc;
+        }
+    }
+}
+
+// y = f / D for the supernode's own columns (the diagonal step of the solve).
+template <class Cv>
+__global__ void k_fwd_finish(const int* __restrict__ fronts, SolveArgs A, const double* __restrict__ diag,
+                             const Cv* __restrict__ fv, Cv* __restrict__ work) {
+    const int s = fronts[blockIdx.x];
+    const SnDev d = A.sn[s];
+    for (int r = 0; r < A.nrhs; ++r) {
+        const Cv* f = fv + A.fvec_off[s] + r * A.fv_stride;
+        for (int a = threadIdx.x; a < d.w; a += blockDim.x)
+            work[d.first_col + a + (long long)r * A.ldw] = (Cv)((double)f[a] / diag[d.first_col + a]);
+    }
+}
+
+template <class Cv>
+__global__ void k_bwd_gather(const int* __restrict__ fronts, SolveArgs A, const Cv* __restrict__ work,
+                             Cv* __restrict__ fv) {
+    const int s = fronts[blockIdx.x];
+    const SnDev d = A.sn[s];
+    const int* rows = A.rows + d.rows_off;
+    for (int r = 0; r < A.nrhs; ++r) {
+        Cv* g = fv + A.fvec_off[s] + r * A.fv_stride;
+        for (int a = threadIdx.x; a < d.m; a += blockDim.x) g[a] = work[rows[a] + (long long)r * A.ldw];
+    }
+}
+
+// g[k] -= sum_{i in [r0, r1)} L[i,k] g[i] for columns k in [k0, k0+kn), one warp per column.
+template <class T, class Cv>
+__global__ void k_bwd_cols(const SolveBlockTask* __restrict__ tasks, SolveArgs A, const T* __restrict__ panel,
+                           Cv* __restrict__ fv) {
+    const SolveBlockTask tk = tasks[blockIdx.x];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (warp >= tk.kn) return;
+    const SnDev d = A.sn[tk.s];
+    const int k = tk.k0 + warp;
+    const T* col = panel + d.panel_off + (long long)k * d.ldp;
+    for (int r = 0; r < A.nrhs; ++r) {
+        Cv* g = fv + A.fvec_off[tk.s] + r * A.fv_stride;
+        Cv acc = Cv(0);
+        for (int i = tk.r0 + lane; i < tk.r1; i += 32) acc += (Cv)col[i] * g[i];
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) g[k] -= acc;
+    }
+}
+
+// Unit upper solve with the transposed diagonal block [k0, k0+kn).
+template <class T, class Cv>
+__global__ void k_bwd_diag(const SolveBlockTask* __restrict__ tasks, SolveArgs A, const T* __restrict__ panel,
+                           Cv* __restrict__ fv) {
+    __shared__ Cv Lb[64 * 65];
+    __shared__ Cv x[64];
+    const SolveBlockTask tk = tasks[blockIdx.x];
+    const SnDev d = A.sn[tk.s];
+    const T* P = panel + d.panel_off;
+    const int kn = tk.kn;
+    for (int idx = threadIdx.x; idx < kn * kn; idx += blockDim.x) {
+        int r = idx % kn, c = idx / kn;
+        Lb[r + c * 65] = r > c ? (Cv)P[(tk.k0 + r) + (long long)(tk.k0 + c) * d.ldp] : Cv(0);
+    }
+    for (int r = 0; r < A.nrhs; ++r) {
+        Cv* g = fv + A.fvec_off[tk.s] + r * A.fv_stride + tk.k0;
+        __syncthreads();
+        if (threadIdx.x < kn) x[threadIdx.x] = g[threadIdx.x];
+        __syncthreads();
+        for (int k = kn - 1; k > 0; --k) {
+            const Cv xk = x[k];
+            __syncthreads();
+            int j = threadIdx.x;
+            if (j < k) x[j] -= Lb[k + j * 65] * xk;
+            __syncthreads();
+        }
+        if (threadIdx.x < kn) g[threadIdx.x] = x[threadIdx.x];
+    }
+}
+
+template <class Cv>
+__global__ void k_bwd_finish(const int* __restrict__ fronts, SolveArgs A, const Cv* __restrict__ fv,
+                             Cv* __restrict__ work) {
+    const int s = fronts[blockIdx.x];
+    const SnDev d = A.sn[s];
+    for (int r = 0; r < A.nrhs; ++r) {
+        const Cv* g = fv + A.fvec_off[s] + r * A.fv_stride;
+        for (int a = threadIdx.x; a < d.w; a += blockDim.x) work[d.first_col + a + (long long)r * A.ldw] = g[a];
+    }
+}
+
+// ---- FP64 symmetric product through a full (both triangles) CSR ----
+
+// full_val[k] = values[full_src[k]] — refreshed once per factorisation.
+__global__ void k_gather_values(const double* __restrict__ values, const int* __restrict__ src, long long count,
+                                double* __restrict__ out) {
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < count; k += (long long)gridDim.x * blockDim.x)
+        out[k] = values[src[k]];
+}
+
+// r = b - A x (or y = A x when b is null), one warp per row.
+__global__ void k_spmv_residual(const int* __restrict__ ptr, const int* __restrict__ col, const double* __restrict__ val,
+                                int n, int nrhs, const double* __restrict__ x, int ldx, const double* __restrict__ b,
+                                int ldb, double* __restrict__ out, int ldo) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    const int row = warp;
+    if (row >= n) return;
+    const int p0 = ptr[row], p1 = ptr[row + 1];
+    for (int r = 0; r < nrhs; ++r) {
+        const double* xr = x + (long long)r * ldx;
+        double acc = 0.0;
+        for (int p = p0 + lane; p < p1; p += 32) acc += val[p] * xr[col[p]];
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) out[row + (long long)r * ldo] = b ? b[row + (long long)r * ldb] - acc : acc;
+    }
+}
+
+// Deterministic column dot products: stage 1 per-block partial sums.
+constexpr int kDotBlocks = 256;
+__global__ void k_dot_partial(const double* __restrict__ u, int ldu, const double* __restrict__ v, int ldv, int n,
+                              double* __restrict__ partial) {
+    __shared__ double red[256];
+    const int r = blockIdx.y;
+    double acc = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        acc += u[i + (long long)r * ldu] * v[i + (long long)r * ldv];
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x + r * gridDim.x] = red[0];
+}
+__global__ void k_dot_finish(const double* __restrict__ partial, int blocks, int nrhs, double* __restrict__ out) {
+    const int r = threadIdx.x;
+    if (r >= nrhs) return;
+    double s = 0.0;
+    for (int b = 0; b < blocks; ++b) s += partial[b + r * blocks];
+    out[r] = s;
+}
+
+// x += alpha_r * p (per column), with alpha read from device memory.
+__global__ void k_axpy_cols(double* __restrict__ x, int ldx, const double* __restrict__ p, int ldp,
+                            const double* __restrict__ alpha, double sign, int n, int nrhs) {
+    for (int r = blockIdx.y; r < nrhs; r += gridDim.y) {
+        const double a = sign * alpha[r];
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+            x[i + (long long)r * ldx] += a * p[i + (long long)r * ldp];
+    }
+}
+
+// p = z + beta_r * p
+__global__ void k_xpby_cols(const double* __restrict__ z, int ldz, double* __restrict__ p, int ldp,
+                            const double* __restrict__ beta, int n, int nrhs) {
+    for (int r = blockIdx.y; r < nrhs; r += gridDim.y) {
+        const double bt = beta[r];
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+            p[i + (long long)r * ldp] = z[i + (long long)r * ldz] + bt * p[i + (long long)r * ldp];
+    }
+}
+
+}  // namespace uchol_dev

@@ -1,0 +1,459 @@
+"""The UCHOL direct solver with its numeric phase on the GPU.
+
+Python mirror of the reference's public API for this path:
+
+* ``UtduSolverOptions``, ``FillReducingOrdering`` CAESolvers/UCHOL/UtduSymbolicFactorization.cs:8-98
+* ``UtduSymbolicFactorization``                   CAESolvers/UCHOL/UtduSymbolicFactorization.cs:109-320
+* ``UtduNumericFactorization``                    CAESolvers/UCHOL/UtduNumericFactorization.cs:24-235
+* ``SymmetricUtduSolver``                         CAESolvers/UCHOL/SymmetricUtduSolver.cs:45-109
+* ``LinearSolver`` / ``DirectLinearSolver``       CAESolvers/LinearSolver.cs:7-31, DirectLinearSolver.cs:6
+* ``ResidualCalculator``                          CAESolvers/ResidualCalculator.cs:3-31
+
+The symbolic phase runs on the host (libuchol_host.so, the same integer
+arrays the reference computes); ``Factorize`` and ``Solve`` run on the GPU
+through libuchol_gpu.so.  There is no CPU numeric path.
+
+GPU extensions of the options: ``Precision`` (FP64 — the plain form — or the
+mixed TF32/BF16 forms whose Schur updates run on tensor cores), the outer
+block of the tensor-core update, and the refinement tolerance used by
+``Solve`` on a mixed-precision factor.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import enum
+import os
+
+import numpy as np
+
+from . import _native
+from .errors import (ArgumentException, ArgumentNullException, InvalidOperationException, raise_for_status)
+from .matrix import LinearSystem, SymmetricCSRMatrix
+
+
+class FillReducingOrdering(enum.IntEnum):
+    Natural = 0
+    ApproximateMinimumDegree = 1
+
+
+class Precision(enum.IntEnum):
+    FP64 = _native.PRECISION_FP64
+    TF32 = _native.PRECISION_TF32
+    BF16 = _native.PRECISION_BF16
+
+
+class UtduSolverOptions:
+    def __init__(self, **kw):
+        self.Ordering = FillReducingOrdering.ApproximateMinimumDegree
+        self.MaxDegreeOfParallelism = 0
+        self.SupernodeAmalgamationLimit = 64
+        self.PanelWidth = 32
+        self.AllowDiagonalRegularization = True
+        self.PivotTolerance = 1e-13
+        self.DiagonalRegularization = 1e-10
+        self.ParallelUpdateThreshold = 1 << 20
+        # device extensions
+        self.Precision = Precision.FP64
+        self.BlockWidth = 0
+        self.RefinementTolerance = 1e-12
+        self.RefinementMaxIterations = 50
+        for k, v in kw.items():
+            if not hasattr(self, k):
+                raise AttributeError(f"unknown option {k}")
+            setattr(self, k, v)
+
+    def ResolveWorkerCount(self) -> int:
+        requested = self.MaxDegreeOfParallelism if self.MaxDegreeOfParallelism > 0 else (os.cpu_count() or 1)
+        return max(1, requested)
+
+    def ResolvePanelWidth(self) -> int:
+        return min(128, max(4, self.PanelWidth))
+
+    def _native_options(self) -> _native.Options:
+        o = _native.Options()
+        o.allow_diagonal_regularization = 1 if self.AllowDiagonalRegularization else 0
+        o.pivot_tolerance = float(self.PivotTolerance)
+        o.diagonal_regularization = float(self.DiagonalRegularization)
+        o.panel_width = int(self.ResolvePanelWidth())
+        o.precision = int(self.Precision)
+        o.block_width = int(self.BlockWidth)
+        return o
+
+
+# Array selectors of uchol_analysis_copy (include/uchol_host.h)
+_A = dict(PERMUTATION=0, INVERSE_PERMUTATION=1, PATTERN_PTR=2, PATTERN_ROWS=3, LOWER_START=4, LOWER_VALUE_PTR=5,
+          LOWER_VALUE_INDEX=6, DIAG_VALUE_INDEX=7, ETREE_PARENT=8, COLUMN_COUNTS=9, FIRST_COLUMN=10, SUPERNODE_OF=11,
+          SN_PARENT=12, CHILD_PTR=13, CHILDREN=14, FRONT_PTR=15, FRONT_ROWS=16, SLAB_INDEX=17, SLAB_OFFSET=18,
+          SLAB_LENGTHS=19)
+
+_FRONT_RETENTION_LIMIT = 1 << 25  # UtduNumericFactorization.cs:264
+
+
+class UtduSymbolicFactorization:
+    """Permutation, factor structure and supernode partition; no matrix values."""
+
+    def __init__(self):
+        raise InvalidOperationException("use UtduSymbolicFactorization.Analyze or SymmetricUtduSolver.Analyze")
+
+    @classmethod
+    def Analyze(cls, matrix: SymmetricCSRMatrix, options: UtduSolverOptions) -> "UtduSymbolicFactorization":
+        if matrix is None:
+            raise ArgumentNullException("matrix")
+        if options is None:
+            raise ArgumentNullException("options")
+        lib = _native.host()
+        h = C.c_void_p()
+        st = lib.uchol_analyze(matrix.Size, matrix.NonZeroCount, _native.ptr(matrix.RowPointers),
+                               _native.ptr(matrix.ColumnIndices), int(options.Ordering),
+                               max(1, int(options.SupernodeAmalgamationLimit)), C.byref(h))
+        raise_for_status(st, lib.uchol_host_last_error())
+        self = cls.__new__(cls)
+        try:
+            info = _native.AnalysisInfo()
+            raise_for_status(lib.uchol_analysis_get_info(h, C.byref(info)), lib.uchol_host_last_error())
+            self._info = info
+            n, S = info.n, info.supernode_count
+            lengths = dict(PERMUTATION=n, INVERSE_PERMUTATION=n, PATTERN_PTR=n + 1, PATTERN_ROWS=info.pattern_entries,
+                           LOWER_START=n, LOWER_VALUE_PTR=n + 1, LOWER_VALUE_INDEX=info.lower_entries,
+                           DIAG_VALUE_INDEX=n, ETREE_PARENT=n, COLUMN_COUNTS=n, FIRST_COLUMN=S + 1, SUPERNODE_OF=n,
+                           SN_PARENT=S, CHILD_PTR=S + 1, CHILDREN=info.child_entries, FRONT_PTR=S + 1,
+                           FRONT_ROWS=info.front_row_entries, SLAB_INDEX=S, SLAB_OFFSET=S,
+                           SLAB_LENGTHS=info.slab_count)
+            self.arrays = {}
+            for name, ln in lengths.items():
+                a = np.zeros(max(0, ln), np.int32)
+                if ln > 0:
+                    raise_for_status(lib.uchol_analysis_copy(h, _A[name], _native.ptr(a)), lib.uchol_host_last_error())
+                self.arrays[name] = a
+        finally:
+            lib.uchol_analysis_destroy(h)
+        self._matrix_row_ptr = matrix.RowPointers.copy()
+        self._matrix_col = matrix.ColumnIndices.copy()
+        self._device = None
+        return self
+
+    # -- public statistics (UtduSymbolicFactorization.cs:127-234) ----------
+    @property
+    def Size(self) -> int:
+        return self._info.n
+
+    @property
+    def Permutation(self) -> np.ndarray:
+        return self.arrays["PERMUTATION"]
+
+    @property
+    def InversePermutation(self) -> np.ndarray:
+        return self.arrays["INVERSE_PERMUTATION"]
+
+    @property
+    def MatrixNonZeroCount(self) -> int:
+        return self._info.nnz
+
+    @property
+    def SupernodeCount(self) -> int:
+        return self._info.supernode_count
+
+    @property
+    def FactorEntryCount(self) -> int:
+        return int(self._info.factor_entry_count)
+
+    @property
+    def StrictFactorNonZeroCount(self) -> int:
+        return int(self._info.strict_factor_nonzero_count)
+
+    @property
+    def FactorOperationCount(self) -> int:
+        return int(self._info.factor_operation_count)
+
+    @property
+    def MaxFrontSize(self) -> int:
+        return self._info.max_front_size
+
+    @property
+    def MaxSupernodeWidth(self) -> int:
+        return self._info.max_supernode_width
+
+    @property
+    def EstimatedFactorBytes(self) -> int:
+        return self.FactorEntryCount * 8
+
+    @property
+    def MaxFrontBytes(self) -> int:
+        m = self.MaxFrontSize
+        return m * (m + 1) // 2 * 8
+
+    @property
+    def PeakContributionBytes(self) -> int:
+        return int(self._info.peak_contribution_entries) * 8
+
+    @property
+    def StructureBytes(self) -> int:
+        return (self._info.pattern_entries + self._info.lower_entries + self._info.front_row_entries) * 4
+
+    def EstimatePeakBytes(self, worker_count: int) -> int:
+        workers = max(1, worker_count)
+        retained = min(self.MaxFrontBytes, _FRONT_RETENTION_LIMIT * 8)
+        return self.EstimatedFactorBytes + self.StructureBytes + self.PeakContributionBytes + workers * retained + \
+            self.MaxFrontBytes
+
+    def EnsureCompatible(self, matrix: SymmetricCSRMatrix) -> None:
+        if matrix.Size != self.Size:
+            raise ArgumentException(f"Matrix size {matrix.Size} does not match the symbolic factorization "
+                                    f"built for {self.Size} equations.")
+        if matrix.NonZeroCount != self.MatrixNonZeroCount:
+            raise ArgumentException(
+                "The matrix sparse structure has changed since symbolic analysis "
+                f"(previously {self.MatrixNonZeroCount} nonzero elements, now {matrix.NonZeroCount}). "
+                "Symbolic factorization can be reused only when the structure is unchanged. Run Analyze again.")
+
+    # -- device upload (once per pattern) --------------------------------------
+    def device_handle(self):
+        if self._device is None:
+            lib = _native.gpu()
+            a = self.arrays
+            d = _native.SymbolicDesc()
+            keep = []
+
+            def p(x):
+                x = np.ascontiguousarray(x, np.int32)
+                keep.append(x)
+                return _native.ptr(x)
+
+            d.n, d.nnz = self.Size, self.MatrixNonZeroCount
+            d.row_ptr, d.col = p(self._matrix_row_ptr), p(self._matrix_col)
+            d.permutation, d.diag_value_index = p(a["PERMUTATION"]), p(a["DIAG_VALUE_INDEX"])
+            d.pattern_ptr, d.pattern_rows = p(a["PATTERN_PTR"]), p(a["PATTERN_ROWS"])
+            d.lower_start, d.lower_value_ptr = p(a["LOWER_START"]), p(a["LOWER_VALUE_PTR"])
+            d.lower_value_index = p(a["LOWER_VALUE_INDEX"])
+            d.supernode_count = self.SupernodeCount
+            d.first_column, d.parent = p(a["FIRST_COLUMN"]), p(a["SN_PARENT"])
+            d.child_ptr, d.children = p(a["CHILD_PTR"]), p(a["CHILDREN"])
+            d.front_ptr, d.front_rows = p(a["FRONT_PTR"]), p(a["FRONT_ROWS"])
+            h = C.c_void_p()
+            raise_for_status(lib.uchol_symbolic_create(C.byref(d), C.byref(h)), lib.uchol_last_error())
+            self._device = h
+        return self._device
+
+    def __del__(self):
+        h = getattr(self, "_device", None)
+        if h is not None and _native._GPU is not None:
+            _native._GPU.uchol_symbolic_destroy(h)
+            self._device = None
+
+
+class UtduNumericFactorization:
+    """A = U^T D U on the GPU; Solve handles any number of right-hand sides."""
+
+    def __init__(self, symbolic: UtduSymbolicFactorization, handle, stats: _native.FactorStats,
+                 options: UtduSolverOptions, matrix: SymmetricCSRMatrix):
+        self._symbolic = symbolic
+        self._h = handle
+        self._stats = stats
+        self._options = options
+        self._nnz = matrix.NonZeroCount
+        self._diag = None
+        self.LastRefinement = None
+
+    @property
+    def Symbolic(self) -> UtduSymbolicFactorization:
+        return self._symbolic
+
+    @property
+    def Size(self) -> int:
+        return self._symbolic.Size
+
+    @property
+    def RegularizedPivotCount(self) -> int:
+        return self._stats.regularized_pivot_count
+
+    @property
+    def NegativePivotCount(self) -> int:
+        return self._stats.negative_pivot_count
+
+    @property
+    def SmallestPivotMagnitude(self) -> float:
+        return self._stats.smallest_pivot_magnitude
+
+    @property
+    def LargestPivotMagnitude(self) -> float:
+        return self._stats.largest_pivot_magnitude
+
+    @property
+    def IsPositiveDefinite(self) -> bool:
+        return self.RegularizedPivotCount == 0 and self.NegativePivotCount == 0
+
+    @property
+    def Precision(self) -> Precision:
+        return Precision(self._options.Precision)
+
+    @property
+    def FactorMilliseconds(self) -> float:
+        return self._stats.factor_ms
+
+    @property
+    def DeviceBytes(self) -> int:
+        return int(self._stats.device_bytes)
+
+    @property
+    def Diagonal(self) -> np.ndarray:
+        if self._diag is None:
+            lib = _native.gpu()
+            d = np.zeros(self.Size, np.float64)
+            raise_for_status(lib.uchol_factor_diagonal(self._h, _native.ptr(d, C.c_double)), lib.uchol_last_error())
+            self._diag = d
+        return self._diag
+
+    def Solve(self, right_hand_side) -> np.ndarray:
+        """x = A^-1 b (b may be a vector or an n x k block of right-hand sides).
+
+        A FP64 factor is applied once, as in the reference.  A mixed-precision
+        factor is refined against the FP64 matrix until the relative residual
+        of every column reaches ``RefinementTolerance``.
+        """
+        if right_hand_side is None:
+            raise ArgumentNullException("rightHandSide")
+        b = np.asarray(right_hand_side, dtype=np.float64)
+        n = self.Size
+        if b.shape[0] != n:
+            raise ArgumentException(f"The right-hand side length {b.shape[0]} does not match the matrix size {n}.")
+        if self.Precision != Precision.FP64:
+            return self.SolveRefined(b, self._options.RefinementTolerance, self._options.RefinementMaxIterations)
+        return self._apply(b)
+
+    def _apply(self, b):
+        lib = _native.gpu()
+        vec = b.ndim == 1
+        B = np.asfortranarray(b.reshape(b.shape[0], -1))
+        X = np.zeros_like(B, order="F")
+        k = B.shape[1]
+        ld = max(1, B.shape[0])
+        st = lib.uchol_solve(self._h, self.Size, k, _native.ptr(B, C.c_double), ld, _native.ptr(X, C.c_double), ld)
+        raise_for_status(st, lib.uchol_last_error())
+        return X[:, 0].copy() if vec else X
+
+    def SolveRefined(self, right_hand_side, tolerance: float = 1e-10, max_iterations: int = 50, method: int = 0):
+        """Solve with FP64-residual refinement; statistics land in ``LastRefinement``."""
+        lib = _native.gpu()
+        b = np.asarray(right_hand_side, dtype=np.float64)
+        if b.shape[0] != self.Size:
+            raise ArgumentException(f"The right-hand side length {b.shape[0]} does not match the matrix size {self.Size}.")
+        vec = b.ndim == 1
+        B = np.asfortranarray(b.reshape(b.shape[0], -1))
+        X = np.zeros_like(B, order="F")
+        ro = _native.RefineOptions(float(tolerance), int(max_iterations), int(method))
+        rs = _native.RefineStats()
+        ld = max(1, B.shape[0])
+        st = lib.uchol_solve_refined(self._h, self.Size, B.shape[1], _native.ptr(B, C.c_double), ld,
+                                     _native.ptr(X, C.c_double), ld, C.byref(ro), C.byref(rs))
+        self.LastRefinement = rs
+        raise_for_status(st, lib.uchol_last_error())
+        return X[:, 0].copy() if vec else X
+
+    def DeviceResidualNorms(self, b, x) -> np.ndarray:
+        """||b - A x||_2 per column with the device FP64 product."""
+        lib = _native.gpu()
+        B = np.asfortranarray(np.asarray(b, np.float64).reshape(self.Size, -1))
+        X = np.asfortranarray(np.asarray(x, np.float64).reshape(self.Size, -1))
+        out = np.zeros(B.shape[1])
+        ld = max(1, self.Size)
+        st = lib.uchol_residual_norms(self._h, self.Size, B.shape[1], _native.ptr(B, C.c_double), ld,
+                                      _native.ptr(X, C.c_double), ld, _native.ptr(out, C.c_double))
+        raise_for_status(st, lib.uchol_last_error())
+        return out
+
+    def Refactorize(self, matrix: SymmetricCSRMatrix) -> None:
+        """New values, same pattern, same device storage."""
+        self._symbolic.EnsureCompatible(matrix)
+        lib = _native.gpu()
+        vals = np.ascontiguousarray(matrix.Values, np.float64)
+        st = lib.uchol_refactorize(self._h, vals.ctypes.data_as(C.c_void_p), 0, C.byref(self._stats))
+        raise_for_status(st, lib.uchol_last_error())
+        self._diag = None
+
+    @staticmethod
+    def ResidualNorm(matrix: SymmetricCSRMatrix, right_hand_side, solution) -> float:
+        """||b - A x||_2 in FP64 (UtduNumericFactorization.cs:222-234)."""
+        product = matrix.Multiply(solution)
+        d = np.asarray(right_hand_side, np.float64) - product
+        return float(np.sqrt(np.sum(d * d)))
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and _native._GPU is not None:
+            _native._GPU.uchol_factor_destroy(h)
+            self._h = None
+
+
+class LinearSolver:
+    """Type-checked dispatch from a LinearSystem to SolveCore (CAESolvers/LinearSolver.cs:7-31)."""
+
+    MatrixType = SymmetricCSRMatrix
+
+    def Solve(self, system: LinearSystem) -> np.ndarray:
+        if system is None:
+            raise ArgumentNullException("system")
+        matrix = self.GetMatrix(system)
+        return self.SolveCore(matrix, system.RightHandSide)
+
+    def GetMatrix(self, system: LinearSystem):
+        if system is None:
+            raise ArgumentNullException("system")
+        if not isinstance(system.Matrix, self.MatrixType):
+            raise ArgumentException(f"The solver supports {self.MatrixType.__name__}, but "
+                                    f"{type(system.Matrix).__name__} was provided.", "system")
+        return system.Matrix
+
+    def SolveCore(self, matrix, right_hand_side):
+        raise NotImplementedError
+
+
+class DirectLinearSolver(LinearSolver):
+    pass
+
+
+class SymmetricUtduSolver(DirectLinearSolver):
+    """Direct solver A x = b for SymmetricCSRMatrix with A = U^T D U on the GPU."""
+
+    def __init__(self, options: UtduSolverOptions | None = None):
+        if options is None:
+            options = UtduSolverOptions()
+        self.Options = options
+
+    def Analyze(self, matrix: SymmetricCSRMatrix) -> UtduSymbolicFactorization:
+        if matrix is None:
+            raise ArgumentNullException("matrix")
+        return UtduSymbolicFactorization.Analyze(matrix, self.Options)
+
+    def Factorize(self, matrix: SymmetricCSRMatrix, symbolic: UtduSymbolicFactorization | None = None):
+        if matrix is None:
+            raise ArgumentNullException("matrix")
+        if symbolic is None:
+            symbolic = self.Analyze(matrix)
+        else:
+            symbolic.EnsureCompatible(matrix)
+        lib = _native.gpu()
+        h = symbolic.device_handle()
+        out = C.c_void_p()
+        stats = _native.FactorStats()
+        opts = self.Options._native_options()
+        vals = np.ascontiguousarray(matrix.Values, np.float64)
+        st = lib.uchol_factorize(h, matrix.Size, matrix.NonZeroCount, _native.ptr(vals, C.c_double), C.byref(opts),
+                                 C.byref(out), C.byref(stats))
+        raise_for_status(st, lib.uchol_last_error())
+        return UtduNumericFactorization(symbolic, out, stats, self.Options, matrix)
+
+    def SolveCore(self, matrix, right_hand_side):
+        return self.Factorize(matrix).Solve(right_hand_side)
+
+
+class ResidualCalculator:
+    """FP64 residual and vector norms (CAESolvers/ResidualCalculator.cs:5-30)."""
+
+    def CalculateResidualNorm(self, matrix, right_hand_side, solution) -> float:
+        product = matrix.Multiply(solution)
+        r = np.asarray(right_hand_side, np.float64) - product
+        return float(np.sqrt(np.sum(r * r)))
+
+    def CalculateNorm(self, vector) -> float:
+        v = np.asarray(vector, np.float64)
+        return float(np.sqrt(np.sum(v * v)))
