@@ -155,10 +155,27 @@ int uchol_residual_norms(uchol_factor f, int n, int nrhs, const double* b, int l
 
 /* Device-time of the last call on the handle's stream, per phase. */
 typedef struct {
-    double assemble_ms, extend_add_ms, small_fronts_ms, panel_ms, schur_ms, total_ms;
+    double pivot_block_ms, extend_add_ms, small_fronts_ms, panel_ms, schur_ms, total_ms;  /* filled when UCHOL_PHASE_TIMES is set */
     int launches;            /* kernel launches of the last factorisation */
+    double schur_tensor_flops;   /* algorithmic flops of the tensor-core Schur updates (lower triangle) */
+    double schur_tensor_ms;      /* their device time (UCHOL_PHASE_TIMES) */
+    int schur_tensor_launches;
 } uchol_phase_times;
 int uchol_factor_phase_times(uchol_factor f, uchol_phase_times* t);
+
+/* Device memory a factorisation with these options will reserve, computed on
+ * the host from the symbolic arrays alone (no GPU needed): factor panels,
+ * the planned contribution arena and the tensor-core operand staging.
+ * Counterpart of UtduSymbolicFactorization.EstimatePeakBytes
+ * (CAESolvers/UCHOL/UtduSymbolicFactorization.cs:203-219). */
+int uchol_estimate_device_bytes(const uchol_symbolic_desc* desc, const uchol_options* opts, int64_t* factor_bytes,
+                                int64_t* contribution_bytes, int64_t* staging_bytes, int* levels, int* launches);
+
+/* Number of kernel launches this library has issued since it was loaded. */
+int64_t uchol_kernel_launches(void);
+/* Per-phase device timing of factorisations (one CUDA event pair per launch);
+ * also enabled by the environment variable UCHOL_PHASE_TIMES. */
+void uchol_set_phase_timing(int on);
 
 const char* uchol_last_error(void);
 

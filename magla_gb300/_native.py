@@ -84,9 +84,10 @@ class RefineStats(C.Structure):
 
 
 class PhaseTimes(C.Structure):
-    _fields_ = [("assemble_ms", C.c_double), ("extend_add_ms", C.c_double), ("small_fronts_ms", C.c_double),
+    _fields_ = [("pivot_block_ms", C.c_double), ("extend_add_ms", C.c_double), ("small_fronts_ms", C.c_double),
                 ("panel_ms", C.c_double), ("schur_ms", C.c_double), ("total_ms", C.c_double),
-                ("launches", C.c_int)]
+                ("launches", C.c_int), ("schur_tensor_flops", C.c_double), ("schur_tensor_ms", C.c_double),
+                ("schur_tensor_launches", C.c_int)]
 
 
 HOST_SYMBOLS = {
@@ -129,6 +130,10 @@ GPU_SYMBOLS = {
     "uchol_residual_norms": (C.c_int, [C.c_void_p, C.c_int, C.c_int, c_double_p, C.c_int, c_double_p, C.c_int,
                                        c_double_p]),
     "uchol_factor_phase_times": (C.c_int, [C.c_void_p, C.POINTER(PhaseTimes)]),
+    "uchol_estimate_device_bytes": (C.c_int, [C.POINTER(SymbolicDesc), C.POINTER(Options), C.POINTER(C.c_int64),
+                                              C.POINTER(C.c_int64), C.POINTER(C.c_int64), c_int_p, c_int_p]),
+    "uchol_kernel_launches": (C.c_int64, []),
+    "uchol_set_phase_timing": (None, [C.c_int]),
     "uchol_last_error": (C.c_char_p, []),
 }
 

@@ -4,8 +4,10 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <climits>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -25,6 +27,17 @@ using namespace uchol_dev;
 namespace {
 
 thread_local std::string g_error;
+std::atomic<long long> g_launches{0};          // kernel launches issued by this library
+std::atomic<int> g_phase_timing{-1};           // -1: not yet read from UCHOL_PHASE_TIMES
+inline void counted(int k = 1) { g_launches += k; }
+inline bool phase_timing() {
+    int v = g_phase_timing.load();
+    if (v < 0) {
+        v = getenv("UCHOL_PHASE_TIMES") != nullptr ? 1 : 0;
+        g_phase_timing.store(v);
+    }
+    return v != 0;
+}
 
 struct Error : std::runtime_error {
     int code;
@@ -95,7 +108,7 @@ struct DBuf {
 
 struct DevPlan {
     Plan plan;
-    DBuf sn, rel, asm_pos, zero_off, zero_len, ea_items, ea_entries, small, pivot_tasks, panel_tasks, simt_tasks, tc_tasks;
+    DBuf sn, rel, asm_pos, zero_off, zero_len, ea_items, ea_entries, small, pivot_tasks, panel_tasks, simt_jobs, tc_jobs;
     DBuf fvec_off, solve_fronts, solve_tasks;
 };
 
@@ -143,8 +156,8 @@ struct uchol_symbolic_s {
         dp->small.upload(P.small_fronts, stream, "plan");
         dp->pivot_tasks.upload(P.pivot_tasks, stream, "plan");
         dp->panel_tasks.upload(P.panel_tasks, stream, "plan");
-        dp->simt_tasks.upload(P.simt_tasks, stream, "plan");
-        dp->tc_tasks.upload(P.tc_tasks, stream, "plan");
+        dp->simt_jobs.upload(P.simt_jobs, stream, "plan");
+        dp->tc_jobs.upload(P.tc_jobs, stream, "plan");
         dp->fvec_off.upload(P.fvec_off, stream, "plan");
         dp->solve_fronts.upload(P.solve_fronts, stream, "plan");
         dp->solve_tasks.upload(P.solve_tasks, stream, "plan");
@@ -224,10 +237,22 @@ void run_factor_launches(uchol_factor_s* F, cudaStream_t st) {
     FactorCtl* ctl = F->ctl.as<FactorCtl>();
     const SnDev* sn = D.sn.as<SnDev>();
     int launches = 0;
+    // Optional per-kind device timing (UCHOL_PHASE_TIMES=1): one event pair per launch.
+    const bool timing = phase_timing();
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev;
+    std::vector<int> ev_kind;
     size_t small_smem = (size_t)P.max_small_m * P.max_small_m * sizeof(double);
     if (small_smem > 48 * 1024)
         CK(cudaFuncSetAttribute(k_small_fronts<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)small_smem));
     for (const Launch& L : P.launches) {
+        if (timing) {
+            cudaEvent_t a, b;
+            CK(cudaEventCreate(&a));
+            CK(cudaEventCreate(&b));
+            CK(cudaEventRecord(a, st));
+            ev.push_back({a, b});
+            ev_kind.push_back((int)L.kind);
+        }
         switch (L.kind) {
             case Launch::ZeroContrib: {
                 dim3 g(64, std::min(L.count, 65535));
@@ -265,21 +290,43 @@ void run_factor_launches(uchol_factor_s* F, cudaStream_t st) {
             }
             case Launch::SimtUpdate:
                 if (sizeof(T) == 8)
-                    k_simt_update<T, double><<<L.count, 256, 0, st>>>(D.simt_tasks.as<TileTask>() + L.begin, sn, panel,
-                                                                      contrib, diag);
+                    k_simt_update<T, double><<<(unsigned)L.tiles, 256, 0, st>>>(D.simt_jobs.as<UpdJob>() + L.begin,
+                                                                                L.count, sn, panel, contrib, diag);
                 else
-                    k_simt_update<T, float><<<L.count, 256, 0, st>>>(D.simt_tasks.as<TileTask>() + L.begin, sn, panel,
-                                                                     contrib, diag);
+                    k_simt_update<T, float><<<(unsigned)L.tiles, 256, 0, st>>>(D.simt_jobs.as<UpdJob>() + L.begin,
+                                                                               L.count, sn, panel, contrib, diag);
                 break;
             case Launch::TcUpdate:
-                launch_tc_update(F->precision == UCHOL_PRECISION_BF16, D.tc_tasks.as<TileTask>() + L.begin, L.count, sn,
-                                 (float*)panel, (float*)contrib, F->maps, P.cfg.outer_block, &stats->status, st);
+                launch_tc_update(F->precision == UCHOL_PRECISION_BF16, D.tc_jobs.as<UpdJob>() + L.begin, L.count, L.tiles,
+                                 sn, (float*)panel, (float*)contrib, F->maps, P.cfg.outer_block, &stats->status, st);
                 break;
         }
+        if (timing) CK(cudaEventRecord(ev.back().second, st));
         ++launches;
+        counted();
     }
     CK(cudaGetLastError());
     F->phases.launches = launches;
+    F->phases.schur_tensor_flops = P.tc_flops;
+    F->phases.schur_tensor_launches = 0;
+    for (const Launch& L : P.launches) F->phases.schur_tensor_launches += L.kind == Launch::TcUpdate;
+    if (timing) {
+        CK(cudaStreamSynchronize(st));
+        double sum[8] = {0};
+        for (size_t q = 0; q < ev.size(); ++q) {
+            float ms = 0.f;
+            CK(cudaEventElapsedTime(&ms, ev[q].first, ev[q].second));
+            sum[ev_kind[q]] += ms;
+            cudaEventDestroy(ev[q].first);
+            cudaEventDestroy(ev[q].second);
+        }
+        F->phases.extend_add_ms = sum[Launch::ExtendAdd] + sum[Launch::ZeroContrib];
+        F->phases.small_fronts_ms = sum[Launch::SmallFronts];
+        F->phases.panel_ms = sum[Launch::PivotBlock] + sum[Launch::Trsm];
+        F->phases.schur_ms = sum[Launch::SimtUpdate] + sum[Launch::TcUpdate];
+        F->phases.pivot_block_ms = sum[Launch::PivotBlock];
+        F->phases.schur_tensor_ms = sum[Launch::TcUpdate];
+    }
 }
 
 // Full-matrix product structure (both triangles) for the FP64 residual.
@@ -324,12 +371,15 @@ void factorize_impl(uchol_factor_s* F, const double* values, bool on_device) {
     CK(cudaMemsetAsync(stats, 0, sizeof(PivotStats), st));
     if (S->n > 0) {
         k_diag_scale<<<grid_for(S->n, 256), 256, 0, st>>>(F->values.as<double>(), S->d_diag_idx.as<int>(), S->n, stats);
+        counted();
     }
     k_finish_scale<<<1, 1, 0, st>>>(stats, F->ctl.as<FactorCtl>(), F->opts.pivot_tolerance,
                                     F->opts.diagonal_regularization, F->opts.allow_diagonal_regularization);
+    counted();
     if (S->full_nnz > 0)
         k_gather_values<<<grid_for(S->full_nnz, 256), 256, 0, st>>>(F->values.as<double>(), S->d_full_src.as<int>(),
                                                                      S->full_nnz, F->full_val.as<double>());
+    if (S->full_nnz > 0) counted();
     if (S->count > 0) {
         CK(cudaMemsetAsync(F->panel.p, 0, F->panel.bytes, st));
         if (F->elem == 8)
@@ -338,6 +388,7 @@ void factorize_impl(uchol_factor_s* F, const double* values, bool on_device) {
         else
             k_assemble<float><<<grid_for(S->nnz, 256), 256, 0, st>>>(F->values.as<double>(), F->dp->asm_pos.as<long long>(),
                                                                      S->nnz, F->panel.as<float>());
+        counted();
         if (F->elem == 8) run_factor_launches<double>(F, st);
         else run_factor_launches<float>(F, st);
     }
@@ -445,6 +496,7 @@ void run_solve(uchol_factor_s* F, int nrhs, Cv* work, Cv* fv) {
             case SolveLaunch::FwdFinish: k_fwd_finish<Cv><<<L.count, 128, 0, st>>>(fronts + L.begin, A, diag, fv, work); break;
             default: break;
         }
+        counted();
     }
     for (const SolveLaunch& L : P.bwd_launches) {
         if (L.count == 0) continue;
@@ -456,6 +508,7 @@ void run_solve(uchol_factor_s* F, int nrhs, Cv* work, Cv* fv) {
             case SolveLaunch::BwdFinish: k_bwd_finish<Cv><<<L.count, 128, 0, st>>>(fronts + L.begin, A, fv, work); break;
             default: break;
         }
+        counted();
     }
     CK(cudaGetLastError());
 }
@@ -484,11 +537,13 @@ void apply_factor(uchol_factor_s* F, int nrhs, const double* b, int ldb, double*
         k_permute_in<double><<<g, 256, 0, st>>>(b, ldb, S->d_perm.as<int>(), n, nrhs, work, n);
         if (S->count) run_solve<double, double>(F, nrhs, work, F->fv.as<double>());
         k_permute_out<double><<<g, 256, 0, st>>>(work, n, S->d_perm.as<int>(), n, nrhs, x, ldx);
+        counted(2);
     } else {
         float* work = F->work.as<float>();
         k_permute_in<float><<<g, 256, 0, st>>>(b, ldb, S->d_perm.as<int>(), n, nrhs, work, n);
         if (S->count) run_solve<float, float>(F, nrhs, work, F->fv.as<float>());
         k_permute_out<float><<<g, 256, 0, st>>>(work, n, S->d_perm.as<int>(), n, nrhs, x, ldx);
+        counted(2);
     }
     CK(cudaGetLastError());
 }
@@ -498,6 +553,7 @@ void residual(uchol_factor_s* F, int nrhs, const double* x, int ldx, const doubl
     if (S->n == 0) return;
     k_spmv_residual<<<(S->n + 7) / 8, 256, 0, S->stream>>>(S->d_full_ptr.as<int>(), S->d_full_col.as<int>(),
                                                           F->full_val.as<double>(), S->n, nrhs, x, ldx, b, ldb, r, ldr);
+    counted();
 }
 
 // out[r] = u_r . v_r (deterministic two-stage reduction) on the device.
@@ -507,6 +563,7 @@ void dots(uchol_factor_s* F, int nrhs, const double* u, int ldu, const double* v
     dim3 g(kDotBlocks, nrhs);
     k_dot_partial<<<g, 256, 0, S->stream>>>(u, ldu, v, ldv, S->n, partial);
     k_dot_finish<<<1, 32 * ((nrhs + 31) / 32), 0, S->stream>>>(partial, kDotBlocks, nrhs, out);
+    counted(2);
 }
 
 __global__ void k_fill(double* p, double v, int n) {
@@ -565,10 +622,10 @@ void solve_refined(uchol_factor_s* F, int nrhs, const double* b, int ldb, double
     initial = current = rel_max();
     if (method == 1) {
         double* ones = sc + 15 * nrhs;
-        k_fill<<<(nrhs + 31) / 32, 32, 0, st>>>(ones, 1.0, nrhs);
+        k_fill<<<(nrhs + 31) / 32, 32, 0, st>>>(ones, 1.0, nrhs); counted();
         while (current > opt.tolerance && it < opt.max_iterations) {
             apply_factor(F, nrhs, r, n, z, n);
-            k_axpy_cols<<<g, 256, 0, st>>>(x, ldx, z, n, ones, 1.0, n, nrhs);
+            k_axpy_cols<<<g, 256, 0, st>>>(x, ldx, z, n, ones, 1.0, n, nrhs); counted();
             residual(F, nrhs, x, ldx, b, ldb, r, n);
             dots(F, nrhs, r, n, r, n, rnorm2);
             current = rel_max();
@@ -582,9 +639,9 @@ void solve_refined(uchol_factor_s* F, int nrhs, const double* b, int ldb, double
         while (current > opt.tolerance && it < opt.max_iterations) {
             residual(F, nrhs, p, n, nullptr, 0, q, n);   // q = A p
             dots(F, nrhs, p, n, q, n, pq);
-            k_cg_scalars<<<1, 32 * ((nrhs + 31) / 32), 0, st>>>(rz, pq, alpha, nrhs);
-            k_axpy_cols<<<g, 256, 0, st>>>(x, ldx, p, n, alpha, 1.0, n, nrhs);
-            k_axpy_cols<<<g, 256, 0, st>>>(r, n, q, n, alpha, -1.0, n, nrhs);
+            k_cg_scalars<<<1, 32 * ((nrhs + 31) / 32), 0, st>>>(rz, pq, alpha, nrhs); counted();
+            k_axpy_cols<<<g, 256, 0, st>>>(x, ldx, p, n, alpha, 1.0, n, nrhs); counted();
+            k_axpy_cols<<<g, 256, 0, st>>>(r, n, q, n, alpha, -1.0, n, nrhs); counted();
             ++it;
             // true residual for the stopping test (FP64 product, no drift)
             residual(F, nrhs, x, ldx, b, ldb, z, n);
@@ -593,8 +650,8 @@ void solve_refined(uchol_factor_s* F, int nrhs, const double* b, int ldb, double
             if (current <= opt.tolerance) break;
             apply_factor(F, nrhs, r, n, z, n);
             dots(F, nrhs, r, n, z, n, rz_new);
-            k_cg_scalars<<<1, 32 * ((nrhs + 31) / 32), 0, st>>>(rz_new, rz, beta, nrhs);
-            k_xpby_cols<<<g, 256, 0, st>>>(z, n, p, n, beta, n, nrhs);
+            k_cg_scalars<<<1, 32 * ((nrhs + 31) / 32), 0, st>>>(rz_new, rz, beta, nrhs); counted();
+            k_xpby_cols<<<g, 256, 0, st>>>(z, n, p, n, beta, n, nrhs); counted();
             CK(cudaMemcpyAsync(rz, rz_new, nrhs * sizeof(double), cudaMemcpyDeviceToDevice, st));
         }
     }
@@ -612,6 +669,10 @@ void solve_refined(uchol_factor_s* F, int nrhs, const double* b, int ldb, double
 extern "C" {
 
 const char* uchol_last_error(void) { return g_error.c_str(); }
+
+int64_t uchol_kernel_launches(void) { return g_launches.load(); }
+
+void uchol_set_phase_timing(int on) { g_phase_timing.store(on ? 1 : 0); }
 
 void uchol_default_options(uchol_options* o) {
     if (!o) return;
@@ -706,6 +767,34 @@ int uchol_symbolic_create(const uchol_symbolic_desc* d, uchol_symbolic* out) {
             CK(cudaStreamSynchronize(S->stream));
         }
         *out = S.release();
+    });
+}
+
+int uchol_estimate_device_bytes(const uchol_symbolic_desc* d, const uchol_options* opts, int64_t* factor_bytes,
+                                int64_t* contribution_bytes, int64_t* staging_bytes, int* levels, int* launches) {
+    return guarded([&] {
+        if (!d) throw Error(UCHOL_BAD_ARG, "null argument");
+        check_options(opts);
+        uchol_options o;
+        if (opts) o = *opts; else uchol_default_options(&o);
+        PlanConfig cfg = config_for(o);
+        const int n = d->n, count = d->supernode_count;
+        if (n < 0 || count < 0) throw Error(UCHOL_BAD_ARG, "negative size");
+        Plan P;
+        try {
+            P = build_plan(n, count, d->first_column, d->parent, d->child_ptr, d->children, d->front_ptr, d->front_rows,
+                           d->diag_value_index, d->pattern_ptr, d->pattern_rows, d->lower_start, d->lower_value_ptr,
+                           d->lower_value_index, d->nnz, cfg);
+        } catch (const std::runtime_error& e) {
+            throw Error(UCHOL_BAD_ARG, std::string("inconsistent symbolic factorization: ") + e.what());
+        }
+        const int64_t elem = o.precision == UCHOL_PRECISION_FP64 ? 8 : 4;
+        const int64_t op = o.precision == UCHOL_PRECISION_BF16 ? 2 : 4;
+        if (factor_bytes) *factor_bytes = P.factor_elems * elem;
+        if (contribution_bytes) *contribution_bytes = P.contrib_elems * elem;
+        if (staging_bytes) *staging_bytes = cfg.tensor_core ? 2 * P.stage_rows * cfg.outer_block * op : 0;
+        if (levels) *levels = P.levels;
+        if (launches) *launches = (int)P.launches.size();
     });
 }
 

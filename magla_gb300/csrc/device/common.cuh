@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <math.h>
 #include <stdint.h>
 
 namespace uchol_dev {
@@ -65,10 +66,70 @@ struct TileTask {      // C[i0:i0+TM, j0:j0+TN] -= sum_k A[i,k] B[j,k], k in [k0
     int jend;          // column limit of this tile (does not cross the panel/contrib split)
 };
 
+// All tiles of one rank-kn update of front s: result columns [c0, cend),
+// rows from each tile's first column down to m, lower triangle only.
+// Column tiles are T wide and restart at the panel/contribution split w, so
+// a tile never spans both storage pieces.  tile_begin is the prefix of tile
+// counts inside one launch; a CTA decodes its tile from blockIdx.x.
+struct UpdJob {
+    long long tile_begin;
+    int s, c0, cend, k0, kn;
+    int stage_row0;    // staging row of front row c0 (tensor-core path), -1 otherwise
+};
+
+// Tiles of a region of nc column tiles whose first row tile count is R:
+// column tile j holds R - j row tiles.
+__host__ __device__ __forceinline__ long long region_tiles(long long nc, long long R) {
+    return nc * R - nc * (nc - 1) / 2;
+}
+
+#ifdef __CUDACC__
+// Decodes tile t of job J (front d) for tile edge T into (i0, j0, jend).
+__device__ __forceinline__ void decode_tile(const UpdJob& J, const SnDev& d, int T, long long t, int& i0, int& j0,
+                                            int& jend) {
+    const int split = d.w;
+    int base = J.c0, lim = J.cend;
+    if (J.c0 < split && split < J.cend) {
+        const int l1 = split - J.c0;
+        const long long nc1 = (l1 + T - 1) / T;
+        const long long R1 = (d.m - J.c0 + T - 1) / T;
+        const long long n1 = region_tiles(nc1, R1);
+        if (t < n1) {
+            lim = split;
+        } else {
+            t -= n1;
+            base = split;
+        }
+    }
+    const long long R = (d.m - base + T - 1) / T;
+    // largest j with j*R - j(j-1)/2 <= t
+    const double b2 = 2.0 * (double)R + 1.0;
+    long long j = (long long)floor((b2 - sqrt(b2 * b2 - 8.0 * (double)t)) * 0.5);
+    if (j < 0) j = 0;
+    while (j > 0 && region_tiles(j, R) > t) --j;
+    while (region_tiles(j + 1, R) <= t) ++j;
+    const long long it = t - region_tiles(j, R);
+    j0 = base + (int)j * T;
+    i0 = j0 + (int)it * T;
+    jend = min(j0 + T, lim);
+}
+
+__device__ __forceinline__ int find_job(const UpdJob* __restrict__ jobs, int njobs, long long bid) {
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (jobs[mid].tile_begin <= bid) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+#endif  // __CUDACC__
+
+#ifdef __CUDACC__
 __device__ __forceinline__ long long elem_offset(const SnDev& d, int i, int j, bool& in_panel) {
     in_panel = j < d.w;
     return in_panel ? d.panel_off + i + (long long)j * d.ldp
                     : d.contrib_off + (i - d.w) + (long long)(j - d.w) * d.ldc;
 }
+#endif
 
 }  // namespace uchol_dev

@@ -285,14 +285,19 @@ __global__ void __launch_bounds__(128) k_trsm(const PanelTask* __restrict__ task
 // lower triangle only (i >= j).  Compute type C: double on the FP64 path,
 // float for the inner updates of the mixed path.
 template <class T, class C>
-__global__ void __launch_bounds__(256) k_simt_update(const TileTask* __restrict__ tasks, const SnDev* __restrict__ sn,
-                                                     T* __restrict__ panel, T* __restrict__ contrib,
-                                                     const double* __restrict__ diag) {
+__global__ void __launch_bounds__(256) k_simt_update(const UpdJob* __restrict__ jobs, int njobs,
+                                                     const SnDev* __restrict__ sn, T* __restrict__ panel,
+                                                     T* __restrict__ contrib, const double* __restrict__ diag) {
     constexpr int TS = 64, KC = 32;
     __shared__ C As[KC][TS + 1];
     __shared__ C Bs[KC][TS + 1];
-    const TileTask tk = tasks[blockIdx.x];
-    const SnDev d = sn[tk.s];
+    const UpdJob J = jobs[find_job(jobs, njobs, blockIdx.x)];
+    const SnDev d = sn[J.s];
+    TileTask tk;
+    tk.s = J.s;
+    tk.k0 = J.k0;
+    tk.kn = J.kn;
+    decode_tile(J, d, TS, (long long)blockIdx.x - J.tile_begin, tk.i0, tk.j0, tk.jend);
     const T* Pn = panel + d.panel_off;
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
     C acc[4][4];
@@ -330,20 +335,26 @@ __global__ void __launch_bounds__(256) k_simt_update(const TileTask* __restrict_
         }
     }
     const bool in_panel = tk.j0 < d.w;
+    T* base = in_panel ? panel : contrib;
+    long long off[4][4];
+    T old[4][4];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-        const int j = tk.j0 + tx + 16 * q;
-        if (j >= tk.jend) continue;
+    for (int q = 0; q < 4; ++q)
 #pragma unroll
         for (int p = 0; p < 4; ++p) {
+            const int j = tk.j0 + tx + 16 * q;
             const int i = tk.i0 + ty + 16 * p;
-            if (i >= d.m || i < j) continue;
-            long long o = in_panel ? d.panel_off + i + (long long)j * d.ldp
-                                   : d.contrib_off + (i - d.w) + (long long)(j - d.w) * d.ldc;
-            T* base = in_panel ? panel : contrib;
-            base[o] = (T)((C)base[o] - acc[p][q]);
+            const bool ok = j < tk.jend && i < d.m && i >= j;
+            off[p][q] = !ok ? -1
+                            : in_panel ? d.panel_off + i + (long long)j * d.ldp
+                                       : d.contrib_off + (i - d.w) + (long long)(j - d.w) * d.ldc;
+            old[p][q] = ok ? base[off[p][q]] : T(0);   // loads first, then stores: no serialised round trips
         }
-    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+#pragma unroll
+        for (int p = 0; p < 4; ++p)
+            if (off[p][q] >= 0) base[off[p][q]] = (T)((C)old[p][q] - acc[p][q]);
 }
 
 }  // namespace uchol_dev

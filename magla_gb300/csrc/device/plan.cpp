@@ -67,6 +67,25 @@ private:
     long long top_ = 0, peak_ = 0;
 };
 
+// Useful flops of an update job: 2 * kn per lower-triangle entry of columns [c0, cend), rows j..m-1.
+double job_flops(const UpdJob& J, const SnDev& d) {
+    const double cols = J.cend - J.c0;
+    const double entries = cols * d.m - (double)(J.c0 + J.cend - 1) * cols / 2.0;
+    return 2.0 * J.kn * entries;
+}
+
+// Tile count of an update job (must match decode_tile).
+long long job_tiles(const UpdJob& J, const SnDev& d, int T) {
+    auto region = [&](int base, int lim) -> long long {
+        if (lim <= base) return 0;
+        long long nc = (lim - base + T - 1) / T;
+        long long R = (d.m - base + T - 1) / T;
+        return region_tiles(nc, R);
+    };
+    if (J.c0 < d.w && d.w < J.cend) return region(J.c0, d.w) + region(d.w, J.cend);
+    return region(J.c0, J.cend);
+}
+
 }  // namespace
 
 Plan build_plan(int n, int count, const int* first_column, const int* parent, const int* child_ptr,
@@ -288,7 +307,8 @@ Plan build_plan(int n, int count, const int* first_column, const int* parent, co
             for (int j0r = 0; j0r < NB; j0r += PB) {
                 int qb = (int)P.pivot_tasks.size();
                 int pb = (int)P.panel_tasks.size();
-                int ub = (int)P.simt_tasks.size();
+                int ub = (int)P.simt_jobs.size();
+                long long utiles = 0;
                 for (int s : large) {
                     const SnDev& d = P.sn[s];
                     if (d.w <= k0) continue;
@@ -313,47 +333,38 @@ Plan build_plan(int n, int count, const int* first_column, const int* parent, co
                     }
                     // inner update of the rest of the outer block (tensor-core configuration only)
                     if (NB != PB && j0 + nbi < outer_end) {
-                        for (int jc = j0 + nbi; jc < outer_end; jc += TS) {
-                            int jend = std::min(jc + TS, outer_end);
-                            for (int i0 = jc; i0 < d.m; i0 += TS)
-                                P.simt_tasks.push_back({s, i0, jc, j0, nbi, -1, -1, jend});
-                        }
+                        UpdJob J{utiles, s, j0 + nbi, outer_end, j0, nbi, -1};
+                        utiles += job_tiles(J, d, TS);
+                        P.simt_flops += job_flops(J, d);
+                        P.simt_jobs.push_back(J);
                     }
                 }
                 if ((int)P.pivot_tasks.size() > qb) P.launches.push_back({Launch::PivotBlock, qb, (int)P.pivot_tasks.size() - qb, 0});
                 if ((int)P.panel_tasks.size() > pb) P.launches.push_back({Launch::Trsm, pb, (int)P.panel_tasks.size() - pb, 0});
-                if ((int)P.simt_tasks.size() > ub) P.launches.push_back({Launch::SimtUpdate, ub, (int)P.simt_tasks.size() - ub, 0});
+                if ((int)P.simt_jobs.size() > ub)
+                    P.launches.push_back({Launch::SimtUpdate, ub, (int)P.simt_jobs.size() - ub, utiles});
                 if (!cfg.tensor_core) break;  // FP64 path: one pivot block per outer step
             }
             // trailing update of the outer step
-            int tb = cfg.tensor_core ? (int)P.tc_tasks.size() : (int)P.simt_tasks.size();
-            for (int s : large) {
-                const SnDev& d = P.sn[s];
-                if (d.w <= k0) continue;
-                int nbo = std::min(NB, d.w - k0);
-                int c0 = k0 + nbo;
-                if (c0 >= d.m) continue;
-                int tn = cfg.tensor_core ? cfg.tc_tile_n : TS;
-                int tm = cfg.tensor_core ? cfg.tc_tile_m : TS;
-                for (int jc = c0; jc < d.m;) {
-                    int split = jc < d.w ? d.w : d.m;   // tiles never straddle the panel/contrib split
-                    int jend = std::min(jc + tn, split);
-                    for (int i0 = jc; i0 < d.m; i0 += tm) {
-                        if (cfg.tensor_core) {
-                            int ar = (int)(stage_base[s] + (i0 - c0));
-                            int br = (int)(stage_base[s] + (jc - c0));
-                            P.tc_tasks.push_back({s, i0, jc, k0, nbo, ar, br, jend});
-                        } else {
-                            P.simt_tasks.push_back({s, i0, jc, k0, nbo, -1, -1, jend});
-                        }
-                    }
-                    jc = jend;
+            {
+                auto& jobs = cfg.tensor_core ? P.tc_jobs : P.simt_jobs;
+                const int T = cfg.tensor_core ? cfg.tc_tile_m : TS;
+                int jb = (int)jobs.size();
+                long long tiles = 0;
+                for (int s : large) {
+                    const SnDev& d = P.sn[s];
+                    if (d.w <= k0) continue;
+                    int nbo = std::min(NB, d.w - k0);
+                    int c0 = k0 + nbo;
+                    if (c0 >= d.m) continue;
+                    UpdJob J{tiles, s, c0, d.m, k0, nbo, cfg.tensor_core ? (int)stage_base[s] : -1};
+                    tiles += job_tiles(J, d, T);
+                    (cfg.tensor_core ? P.tc_flops : P.simt_flops) += job_flops(J, d);
+                    jobs.push_back(J);
                 }
-            }
-            if (cfg.tensor_core) {
-                if ((int)P.tc_tasks.size() > tb) P.launches.push_back({Launch::TcUpdate, tb, (int)P.tc_tasks.size() - tb, 0});
-            } else {
-                if ((int)P.simt_tasks.size() > tb) P.launches.push_back({Launch::SimtUpdate, tb, (int)P.simt_tasks.size() - tb, 0});
+                if ((int)jobs.size() > jb)
+                    P.launches.push_back({cfg.tensor_core ? Launch::TcUpdate : Launch::SimtUpdate, jb,
+                                          (int)jobs.size() - jb, tiles});
             }
         }
     }

@@ -29,7 +29,7 @@ struct Launch {
         ZeroContrib, ExtendAdd, SmallFronts, PivotBlock, Trsm, SimtUpdate, TcUpdate
     } kind;
     int begin, count;   // task range
-    int aux;            // kind-specific (e.g. staging tensor-map index)
+    long long tiles;    // update launches: total tiles (= grid size)
 };
 
 struct SolveLaunch {
@@ -62,11 +62,13 @@ struct Plan {
     std::vector<int> small_fronts;
     std::vector<PanelTask> pivot_tasks;   // one per (front, pivot block)
     std::vector<PanelTask> panel_tasks;   // TRSM row chunks
-    std::vector<TileTask> simt_tasks;
-    std::vector<TileTask> tc_tasks;
+    std::vector<UpdJob> simt_jobs;
+    std::vector<UpdJob> tc_jobs;
     std::vector<Launch> launches;
     int max_small_m = 0;
     long long stage_rows = 0;                  // rows of the operand staging arena (tensor-core path)
+    double tc_flops = 0.0;                     // algorithmic flops of the tensor-core updates (lower triangle)
+    double simt_flops = 0.0;                   // algorithmic flops of the SIMT updates
 
     // solve tasks
     std::vector<int> solve_fronts;             // supernode lists for gather/finish launches

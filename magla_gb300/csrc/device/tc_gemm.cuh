@@ -153,7 +153,7 @@ constexpr int kTcBlockBytes = kTcTile * 128;  // one 128-row x 128-byte K block
 
 template <bool BF16>
 __global__ void __launch_bounds__(128, 1)
-    k_tc_update(const TileTask* __restrict__ tasks, const SnDev* __restrict__ sn, float* __restrict__ panel,
+    k_tc_update(const UpdJob* __restrict__ jobs, int njobs, const SnDev* __restrict__ sn, float* __restrict__ panel,
                 float* __restrict__ contrib, const __grid_constant__ CUtensorMap map_a,
                 const __grid_constant__ CUtensorMap map_b, int max_kblocks, int* status) {
     constexpr int KBE = BF16 ? 64 : 32;  // K elements per 128-byte block
@@ -165,7 +165,15 @@ __global__ void __launch_bounds__(128, 1)
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2);
     int* flag = reinterpret_cast<int*>(tmem_slot + 1);
 
-    const TileTask tk = tasks[blockIdx.x];
+    const UpdJob J = jobs[find_job(jobs, njobs, blockIdx.x)];
+    const SnDev d = sn[J.s];
+    TileTask tk;
+    tk.s = J.s;
+    tk.k0 = J.k0;
+    tk.kn = J.kn;
+    decode_tile(J, d, kTcTile, (long long)blockIdx.x - J.tile_begin, tk.i0, tk.j0, tk.jend);
+    tk.a_row = J.stage_row0 + (tk.i0 - J.c0);
+    tk.b_row = J.stage_row0 + (tk.j0 - J.c0);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nkb = min(max_kblocks, (tk.kn + KBE - 1) / KBE);
 
@@ -217,7 +225,6 @@ __global__ void __launch_bounds__(128, 1)
     }
     tc_fence_after();
     if (done) {
-        const SnDev d = sn[tk.s];
         const bool in_panel = tk.j0 < d.w;
         const int i = tk.i0 + warp * 32 + lane;
         float* base = in_panel ? panel + d.panel_off + i : contrib + d.contrib_off + (i - d.w);
@@ -226,15 +233,18 @@ __global__ void __launch_bounds__(128, 1)
         const bool row_ok = i < d.m;
 #pragma unroll 1
         for (int cc = 0; cc < kTcTile / 32; ++cc) {
-            float v[32];
+            float v[32], old[32];
             tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(cc * 32), v);
+            // all 32 loads are issued before any store so they overlap
 #pragma unroll
             for (int c = 0; c < 32; ++c) {
                 const int j = tk.j0 + cc * 32 + c;
-                if (row_ok && j < tk.jend && i >= j) {
-                    float* p = base + (long long)(j - jshift) * ldc;
-                    *p -= v[c];
-                }
+                old[c] = (row_ok && j < tk.jend && i >= j) ? base[(long long)(j - jshift) * ldc] : 0.f;
+            }
+#pragma unroll
+            for (int c = 0; c < 32; ++c) {
+                const int j = tk.j0 + cc * 32 + c;
+                if (row_ok && j < tk.jend && i >= j) base[(long long)(j - jshift) * ldc] = old[c] - v[c];
             }
         }
     }
@@ -281,16 +291,18 @@ inline void destroy_tc_maps(TcMaps& m) { m.valid = false; }
 
 inline size_t tc_smem_bytes(int kblocks) { return (size_t)kblocks * 2 * kTcBlockBytes + 1024 + 64; }
 
-inline void launch_tc_update(bool bf16, const TileTask* tasks, int count, const SnDev* sn, float* panel, float* contrib,
-                             const TcMaps& maps, int nb, int* status, cudaStream_t st) {
+inline void launch_tc_update(bool bf16, const UpdJob* jobs, int njobs, long long tiles, const SnDev* sn, float* panel,
+                             float* contrib, const TcMaps& maps, int nb, int* status, cudaStream_t st) {
     const int kblocks = nb / (bf16 ? 64 : 32);
     const size_t smem = tc_smem_bytes(kblocks);
     if (bf16) {
         cudaFuncSetAttribute(k_tc_update<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_tc_update<true><<<count, 128, smem, st>>>(tasks, sn, panel, contrib, maps.a, maps.b, kblocks, status);
+        k_tc_update<true><<<(unsigned)tiles, 128, smem, st>>>(jobs, njobs, sn, panel, contrib, maps.a, maps.b, kblocks,
+                                                             status);
     } else {
         cudaFuncSetAttribute(k_tc_update<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_tc_update<false><<<count, 128, smem, st>>>(tasks, sn, panel, contrib, maps.a, maps.b, kblocks, status);
+        k_tc_update<false><<<(unsigned)tiles, 128, smem, st>>>(jobs, njobs, sn, panel, contrib, maps.a, maps.b, kblocks,
+                                                              status);
     }
 }
 

@@ -207,32 +207,57 @@ class UtduSymbolicFactorization:
                 "Symbolic factorization can be reused only when the structure is unchanged. Run Analyze again.")
 
     # -- device upload (once per pattern) --------------------------------------
+    def _desc(self):
+        """The C-ABI view of the symbolic arrays (uchol_symbolic_desc) and the arrays it points into."""
+        a = self.arrays
+        d = _native.SymbolicDesc()
+        keep = []
+
+        def p(x):
+            x = np.ascontiguousarray(x, np.int32)
+            keep.append(x)
+            return _native.ptr(x)
+
+        d.n, d.nnz = self.Size, self.MatrixNonZeroCount
+        d.row_ptr, d.col = p(self._matrix_row_ptr), p(self._matrix_col)
+        d.permutation, d.diag_value_index = p(a["PERMUTATION"]), p(a["DIAG_VALUE_INDEX"])
+        d.pattern_ptr, d.pattern_rows = p(a["PATTERN_PTR"]), p(a["PATTERN_ROWS"])
+        d.lower_start, d.lower_value_ptr = p(a["LOWER_START"]), p(a["LOWER_VALUE_PTR"])
+        d.lower_value_index = p(a["LOWER_VALUE_INDEX"])
+        d.supernode_count = self.SupernodeCount
+        d.first_column, d.parent = p(a["FIRST_COLUMN"]), p(a["SN_PARENT"])
+        d.child_ptr, d.children = p(a["CHILD_PTR"]), p(a["CHILDREN"])
+        d.front_ptr, d.front_rows = p(a["FRONT_PTR"]), p(a["FRONT_ROWS"])
+        return d, keep
+
+    def EstimateDeviceBytes(self, options: UtduSolverOptions | None = None) -> dict:
+        """Device memory of a factorisation with these options (host-side plan, no GPU needed)."""
+        lib = _native.gpu()
+        d, keep = self._desc()
+        o = (options or UtduSolverOptions())._native_options()
+        fb, cb, sb = C.c_int64(), C.c_int64(), C.c_int64()
+        lv, ln = C.c_int(), C.c_int()
+        st = lib.uchol_estimate_device_bytes(C.byref(d), C.byref(o), C.byref(fb), C.byref(cb), C.byref(sb),
+                                             C.byref(lv), C.byref(ln))
+        raise_for_status(st, lib.uchol_last_error())
+        return dict(factor=fb.value, contribution=cb.value, staging=sb.value, levels=lv.value, launches=ln.value)
+
     def device_handle(self):
         if self._device is None:
             lib = _native.gpu()
-            a = self.arrays
-            d = _native.SymbolicDesc()
-            keep = []
-
-            def p(x):
-                x = np.ascontiguousarray(x, np.int32)
-                keep.append(x)
-                return _native.ptr(x)
-
-            d.n, d.nnz = self.Size, self.MatrixNonZeroCount
-            d.row_ptr, d.col = p(self._matrix_row_ptr), p(self._matrix_col)
-            d.permutation, d.diag_value_index = p(a["PERMUTATION"]), p(a["DIAG_VALUE_INDEX"])
-            d.pattern_ptr, d.pattern_rows = p(a["PATTERN_PTR"]), p(a["PATTERN_ROWS"])
-            d.lower_start, d.lower_value_ptr = p(a["LOWER_START"]), p(a["LOWER_VALUE_PTR"])
-            d.lower_value_index = p(a["LOWER_VALUE_INDEX"])
-            d.supernode_count = self.SupernodeCount
-            d.first_column, d.parent = p(a["FIRST_COLUMN"]), p(a["SN_PARENT"])
-            d.child_ptr, d.children = p(a["CHILD_PTR"]), p(a["CHILDREN"])
-            d.front_ptr, d.front_rows = p(a["FRONT_PTR"]), p(a["FRONT_ROWS"])
+            d, keep = self._desc()
             h = C.c_void_p()
             raise_for_status(lib.uchol_symbolic_create(C.byref(d), C.byref(h)), lib.uchol_last_error())
             self._device = h
         return self._device
+
+    def SetStream(self, stream_handle: int | None) -> None:
+        """Runs every device call of this pattern and its factors on the given
+        CUDA stream (a cudaStream_t as an integer; None = a private stream)."""
+        lib = _native.gpu()
+        h = self.device_handle()
+        raise_for_status(lib.uchol_symbolic_set_stream(h, C.c_void_p(stream_handle) if stream_handle else None),
+                         lib.uchol_last_error())
 
     def __del__(self):
         h = getattr(self, "_device", None)
@@ -323,6 +348,8 @@ class UtduNumericFactorization:
     def _apply(self, b):
         lib = _native.gpu()
         vec = b.ndim == 1
+        if self.Size == 0:
+            return np.zeros(b.shape)
         B = np.asfortranarray(b.reshape(b.shape[0], -1))
         X = np.zeros_like(B, order="F")
         k = B.shape[1]
@@ -338,6 +365,9 @@ class UtduNumericFactorization:
         if b.shape[0] != self.Size:
             raise ArgumentException(f"The right-hand side length {b.shape[0]} does not match the matrix size {self.Size}.")
         vec = b.ndim == 1
+        if self.Size == 0:
+            self.LastRefinement = _native.RefineStats()
+            return np.zeros(b.shape)
         B = np.asfortranarray(b.reshape(b.shape[0], -1))
         X = np.zeros_like(B, order="F")
         ro = _native.RefineOptions(float(tolerance), int(max_iterations), int(method))
@@ -361,6 +391,13 @@ class UtduNumericFactorization:
         raise_for_status(st, lib.uchol_last_error())
         return out
 
+    def PhaseTimes(self) -> dict:
+        """Device milliseconds per factorisation phase (filled when UCHOL_PHASE_TIMES is set)."""
+        lib = _native.gpu()
+        t = _native.PhaseTimes()
+        raise_for_status(lib.uchol_factor_phase_times(self._h, C.byref(t)), lib.uchol_last_error())
+        return {name: getattr(t, name) for name, _ in _native.PhaseTimes._fields_}
+
     def Refactorize(self, matrix: SymmetricCSRMatrix) -> None:
         """New values, same pattern, same device storage."""
         self._symbolic.EnsureCompatible(matrix)
@@ -369,6 +406,32 @@ class UtduNumericFactorization:
         st = lib.uchol_refactorize(self._h, vals.ctypes.data_as(C.c_void_p), 0, C.byref(self._stats))
         raise_for_status(st, lib.uchol_last_error())
         self._diag = None
+
+    def RefactorizeDevice(self, d_values: int) -> None:
+        """Refactorise from matrix values already in device memory (pointer as an integer)."""
+        lib = _native.gpu()
+        st = lib.uchol_refactorize(self._h, C.c_void_p(d_values), 1, C.byref(self._stats))
+        raise_for_status(st, lib.uchol_last_error())
+        self._diag = None
+
+    def SolveRefinedDevice(self, d_b: int, d_x: int, nrhs: int = 1, tolerance: float = 1e-10,
+                           max_iterations: int = 100, method: int = 0):
+        """Refined solve on device buffers (column-major n x nrhs, pointers as integers)."""
+        lib = _native.gpu()
+        ro = _native.RefineOptions(float(tolerance), int(max_iterations), int(method))
+        rs = _native.RefineStats()
+        n = max(1, self.Size)
+        st = lib.uchol_solve_refined_device(self._h, self.Size, nrhs, C.c_void_p(d_b), n, C.c_void_p(d_x), n,
+                                            C.byref(ro), C.byref(rs))
+        self.LastRefinement = rs
+        raise_for_status(st, lib.uchol_last_error())
+        return rs
+
+    def SolveDevice(self, d_b: int, d_x: int, nrhs: int = 1) -> None:
+        lib = _native.gpu()
+        n = max(1, self.Size)
+        st = lib.uchol_solve_device(self._h, self.Size, nrhs, C.c_void_p(d_b), n, C.c_void_p(d_x), n)
+        raise_for_status(st, lib.uchol_last_error())
 
     @staticmethod
     def ResidualNorm(matrix: SymmetricCSRMatrix, right_hand_side, solution) -> float:
