@@ -171,6 +171,30 @@ int uchol_factor_phase_times(uchol_factor f, uchol_phase_times* t);
 int uchol_estimate_device_bytes(const uchol_symbolic_desc* desc, const uchol_options* opts, int64_t* factor_bytes,
                                 int64_t* contribution_bytes, int64_t* staging_bytes, int* levels, int* launches);
 
+/* Residual norms without any device allocation.  No counterpart in the
+ * reference: it exists for callers that cannot allocate device memory while
+ * they solve — an application that has reserved all device memory for its
+ * own pool, a caller recording into a CUDA stream capture, or a loop that
+ * must not take the synchronisation of cudaMalloc.  It computes
+ * out[j] = ||b_j - A x_j||_2 for the symmetric matrix given by its upper
+ * triangle (SymmetricCSRMatrix layout: d_row_ptr [n+1], d_col and d_values
+ * [nnz]), with every buffer in device memory and supplied by the caller
+ * (d_norms: nrhs doubles).  Its only scratch is a static device array of
+ * 2^20 doubles (8 MiB, held on every device that loads the library until
+ * exit): n * nrhs + 128 * nrhs must not exceed 2^20 and nrhs must not exceed
+ * 64, otherwise UCHOL_BAD_ARG.  The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress), so make that first call
+ * before any stream capture.  All calls share the array: calls that overlap
+ * on the GPU (other streams, other threads) race and must be serialised by
+ * the caller.  Work is queued on `stream` (cudaStream_t, NULL = default);
+ * results are valid once that stream has completed.  The mirrored half of
+ * the product is accumulated with atomics, so results can differ from call
+ * to call in the last bits. */
+int uchol_residual_norms_static(int n, int nnz, int nrhs, const int* d_row_ptr, const int* d_col,
+                                const double* d_values, const double* d_b, int ldb, const double* d_x, int ldx,
+                                double* d_norms, void* stream);
+const char* uchol_residual_norms_static_error(void);
+
 /* Number of kernel launches this library has issued since it was loaded. */
 int64_t uchol_kernel_launches(void);
 /* Per-phase device timing of factorisations (one CUDA event pair per launch);

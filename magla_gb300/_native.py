@@ -132,6 +132,9 @@ GPU_SYMBOLS = {
     "uchol_factor_phase_times": (C.c_int, [C.c_void_p, C.POINTER(PhaseTimes)]),
     "uchol_estimate_device_bytes": (C.c_int, [C.POINTER(SymbolicDesc), C.POINTER(Options), C.POINTER(C.c_int64),
                                               C.POINTER(C.c_int64), C.POINTER(C.c_int64), c_int_p, c_int_p]),
+    "uchol_residual_norms_static": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                              C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
+    "uchol_residual_norms_static_error": (C.c_char_p, []),
     "uchol_kernel_launches": (C.c_int64, []),
     "uchol_set_phase_timing": (None, [C.c_int]),
     "uchol_last_error": (C.c_char_p, []),

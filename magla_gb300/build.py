@@ -21,7 +21,7 @@ LIB_DIR = ROOT / "_lib"
 OBJ_DIR = ROOT / "_lib" / "obj"
 HOST_SRC = sorted((ROOT / "csrc" / "host").glob("*.cpp"))
 HOST_HDR = sorted((ROOT / "csrc" / "host").glob("*.hpp")) + [REPO / "include" / "uchol_host.h"]
-DEV_CU = [ROOT / "csrc" / "device" / "capi.cu"]
+DEV_CU = [ROOT / "csrc" / "device" / "capi.cu", ROOT / "csrc" / "device" / "static_scratch.cu"]
 DEV_CPP = [ROOT / "csrc" / "device" / "plan.cpp"]
 DEV_HDR = sorted((ROOT / "csrc" / "device").glob("*.cuh")) + sorted((ROOT / "csrc" / "device").glob("*.hpp")) + [
     REPO / "include" / "uchol_gpu.h"
