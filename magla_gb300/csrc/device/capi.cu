@@ -108,8 +108,9 @@ struct DBuf {
 
 struct DevPlan {
     Plan plan;
-    DBuf sn, rel, asm_pos, zero_off, zero_len, ea_items, ea_entries, small, pivot_tasks, panel_tasks, simt_jobs, tc_jobs;
-    DBuf fvec_off, solve_fronts, solve_tasks;
+    DBuf sn, rel, asm_pos, zero_off, zero_len, ea_items, ea_entries, small, pivot_tasks, panel_tasks, simt_jobs, tc_jobs,
+        stage;
+    DBuf fvec_off, solve_fronts, solve_tasks, inv_blocks;
 };
 
 inline int grid_for(long long work, int block, int cap = 152 * 16) {
@@ -134,7 +135,8 @@ struct uchol_symbolic_s {
 
     DevPlan* get_plan(const PlanConfig& c) {
         std::string key = std::to_string(c.pivot_block) + "/" + std::to_string(c.outer_block) + "/" +
-                          std::to_string(c.small_max) + "/" + std::to_string(c.tensor_core);
+                          std::to_string(c.small_max) + "/" + std::to_string(c.tensor_core) + "/" +
+                          std::to_string(c.solve_block);
         auto it = plans.find(key);
         if (it != plans.end()) return it->second.get();
         auto dp = std::make_unique<DevPlan>();
@@ -158,9 +160,11 @@ struct uchol_symbolic_s {
         dp->panel_tasks.upload(P.panel_tasks, stream, "plan");
         dp->simt_jobs.upload(P.simt_jobs, stream, "plan");
         dp->tc_jobs.upload(P.tc_jobs, stream, "plan");
+        dp->stage.upload(P.stage, stream, "plan");
         dp->fvec_off.upload(P.fvec_off, stream, "plan");
         dp->solve_fronts.upload(P.solve_fronts, stream, "plan");
         dp->solve_tasks.upload(P.solve_tasks, stream, "plan");
+        dp->inv_blocks.upload(P.inv_blocks, stream, "plan");
         CK(cudaStreamSynchronize(stream));
         DevPlan* raw = dp.get();
         plans[key] = std::move(dp);
@@ -175,9 +179,18 @@ struct uchol_factor_s {
     int precision = UCHOL_PRECISION_FP64;
     size_t elem = 8;              // bytes per front element
     DBuf panel, contrib, stage_a, stage_b, diag, values, full_val, stats, ctl;
-    DBuf work, fv, vec[6], scal;   // solve workspace
+    DBuf work, fv, fv2, vec[6], scal;   // solve workspace
+    DBuf linv;                          // inverses of the diagonal blocks (solves)
     int ws_nrhs = 0;
-    TcMaps maps;
+    cudaStream_t capture_stream = nullptr;
+    cudaGraphExec_t solve_graph = nullptr;
+    int solve_graph_nrhs = 0, solve_graph_nodes = 0;
+    ~uchol_factor_s() {
+        if (solve_graph) cudaGraphExecDestroy(solve_graph);
+        if (capture_stream) cudaStreamDestroy(capture_stream);
+    }
+    DBuf maps;                    // tensor-map pairs of the staging regions
+    int sms = 148;
     uchol_factor_stats last{};
     uchol_phase_times phases{};
     std::mutex mu;
@@ -212,7 +225,9 @@ PlanConfig config_for(const uchol_options& o) {
     if (o.precision == UCHOL_PRECISION_FP64) {
         c.tensor_core = false;
         c.outer_block = c.pivot_block;
+        c.solve_block = 64;
     } else {
+        c.solve_block = 128;
         c.tensor_core = true;
         c.pivot_block = std::min(c.pivot_block, 32);
         int nb = o.block_width > 0 ? o.block_width : 128;
@@ -278,14 +293,16 @@ void run_factor_launches(uchol_factor_s* F, cudaStream_t st) {
                 if (F->precision == UCHOL_PRECISION_BF16)
                     k_trsm<T, __nv_bfloat16, float, 32><<<L.count, 128, 0, st>>>(
                         tk, sn, panel, diag, F->stage_a.as<__nv_bfloat16>(), F->stage_b.as<__nv_bfloat16>(),
-                        P.cfg.outer_block);
+                        D.stage.as<StageInfo>());
                 else if (F->precision == UCHOL_PRECISION_TF32)
                     k_trsm<T, float, float, 32><<<L.count, 128, 0, st>>>(tk, sn, panel, diag, F->stage_a.as<float>(),
-                                                                          F->stage_b.as<float>(), P.cfg.outer_block);
+                                                                          F->stage_b.as<float>(), D.stage.as<StageInfo>());
                 else if (P.cfg.pivot_block <= 32)
-                    k_trsm<T, T, double, 32><<<L.count, 128, 0, st>>>(tk, sn, panel, diag, nullptr, nullptr, 0);
+                    k_trsm<T, T, double, 32><<<L.count, 128, 0, st>>>(tk, sn, panel, diag, nullptr, nullptr,
+                                                                       D.stage.as<StageInfo>());
                 else
-                    k_trsm<T, T, double, 64><<<L.count, 128, 0, st>>>(tk, sn, panel, diag, nullptr, nullptr, 0);
+                    k_trsm<T, T, double, 64><<<L.count, 128, 0, st>>>(tk, sn, panel, diag, nullptr, nullptr,
+                                                                       D.stage.as<StageInfo>());
                 break;
             }
             case Launch::SimtUpdate:
@@ -297,8 +314,8 @@ void run_factor_launches(uchol_factor_s* F, cudaStream_t st) {
                                                                                L.count, sn, panel, contrib, diag);
                 break;
             case Launch::TcUpdate:
-                launch_tc_update(F->precision == UCHOL_PRECISION_BF16, D.tc_jobs.as<UpdJob>() + L.begin, L.count, L.tiles,
-                                 sn, (float*)panel, (float*)contrib, F->maps, P.cfg.outer_block, &stats->status, st);
+                launch_tc_gemm(F->precision == UCHOL_PRECISION_BF16, D.tc_jobs.as<TcJob>() + L.begin, L.count, L.tiles,
+                               sn, (float*)panel, (float*)contrib, F->maps.as<CUtensorMap>(), &stats->status, F->sms, st);
                 break;
         }
         if (timing) CK(cudaEventRecord(ev.back().second, st));
@@ -327,6 +344,30 @@ void run_factor_launches(uchol_factor_s* F, cudaStream_t st) {
         F->phases.pivot_block_ms = sum[Launch::PivotBlock];
         F->phases.schur_tensor_ms = sum[Launch::TcUpdate];
     }
+}
+
+// Inverses of the diagonal blocks used by the solves (FP64 factor: FP64,
+// 64-wide blocks; FP32 factor: FP32, 128-wide blocks).
+void invert_diagonal_blocks(uchol_factor_s* F, cudaStream_t st) {
+    DevPlan& D = *F->dp;
+    const Plan& P = D.plan;
+    const int nb = (int)P.inv_blocks.size();
+    if (nb == 0) return;
+    if (F->elem == 8) {
+        constexpr int SB = 64;
+        const size_t smem = 2 * SB * SB * sizeof(double);
+        CK(cudaFuncSetAttribute(k_invert_blocks<double, double, SB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_invert_blocks<double, double, SB><<<nb, SB, smem, st>>>(D.inv_blocks.as<SolveBlockTask>(), D.sn.as<SnDev>(),
+                                                                  F->panel.as<double>(), F->linv.as<double>());
+    } else {
+        constexpr int SB = 128;
+        const size_t smem = 2 * SB * SB * sizeof(float);
+        CK(cudaFuncSetAttribute(k_invert_blocks<float, float, SB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_invert_blocks<float, float, SB><<<nb, SB, smem, st>>>(D.inv_blocks.as<SolveBlockTask>(), D.sn.as<SnDev>(),
+                                                                F->panel.as<float>(), F->linv.as<float>());
+    }
+    counted();
+    CK(cudaGetLastError());
 }
 
 // Full-matrix product structure (both triangles) for the FP64 residual.
@@ -391,6 +432,7 @@ void factorize_impl(uchol_factor_s* F, const double* values, bool on_device) {
         counted();
         if (F->elem == 8) run_factor_launches<double>(F, st);
         else run_factor_launches<float>(F, st);
+        invert_diagonal_blocks(F, st);
     }
     PivotStats hs;
     CK(cudaMemcpyAsync(&hs, stats, sizeof(PivotStats), cudaMemcpyDeviceToHost, st));
@@ -447,16 +489,31 @@ uchol_factor_s* create_factor(uchol_symbolic_s* S, int n, int nnz, const uchol_o
     cudaStream_t st = S->stream;
     F->panel.alloc((size_t)P.factor_elems * F->elem, "factor panels");
     F->contrib.alloc((size_t)P.contrib_elems * F->elem, "contribution blocks");
-    if (cfg.tensor_core && P.stage_rows > 0) {
-        size_t op = F->precision == UCHOL_PRECISION_BF16 ? 2 : 4;
-        F->stage_a.alloc((size_t)P.stage_rows * cfg.outer_block * op, "operand staging");
-        F->stage_b.alloc((size_t)P.stage_rows * cfg.outer_block * op, "operand staging");
+    CK(cudaDeviceGetAttribute(&F->sms, cudaDevAttrMultiProcessorCount, S->device));
+    if (cfg.tensor_core && P.stage_elems > 0) {
+        const bool bf16 = F->precision == UCHOL_PRECISION_BF16;
+        const size_t op = bf16 ? 2 : 4;
+        F->stage_a.alloc((size_t)P.stage_elems * op, "operand staging");
+        F->stage_b.alloc((size_t)P.stage_elems * op, "operand staging");
         CK(cudaMemsetAsync(F->stage_a.p, 0, F->stage_a.bytes, st));
         CK(cudaMemsetAsync(F->stage_b.p, 0, F->stage_b.bytes, st));
-        F->maps = make_tc_maps(F->precision == UCHOL_PRECISION_BF16, F->stage_a.p, F->stage_b.p, P.stage_rows,
-                               cfg.outer_block);
+        std::vector<CUtensorMap> maps;
+        maps.reserve(2 * P.map_front.size());
+        for (int s : P.map_front) {
+            const StageInfo& g = P.stage[s];
+            try {
+                maps.push_back(make_region_map(bf16, (char*)F->stage_a.p + g.off * op, P.sn[s].m, g.ld));
+                maps.push_back(make_region_map(bf16, (char*)F->stage_b.p + g.off * op, P.sn[s].m, g.ld));
+            } catch (const std::runtime_error& e) {
+                throw Error(UCHOL_CUDA_ERROR, e.what());
+            }
+        }
+        F->maps.upload(maps, st, "tensor maps");
+        CK(cudaStreamSynchronize(st));
     }
     F->diag.alloc((size_t)std::max(1, S->n) * sizeof(double), "pivots");
+    F->linv.alloc((size_t)std::max<size_t>(1, P.inv_blocks.size()) * cfg.solve_block * cfg.solve_block * F->elem,
+                  "inverse diagonal blocks");
     F->values.alloc((size_t)std::max(1, S->nnz) * sizeof(double), "matrix values");
     F->full_val.alloc((size_t)std::max<long long>(1, S->full_nnz) * sizeof(double), "matrix values");
     F->stats.alloc(sizeof(PivotStats), "statistics");
@@ -466,12 +523,11 @@ uchol_factor_s* create_factor(uchol_symbolic_s* S, int n, int nnz, const uchol_o
 
 // ---- solves ----
 
-template <class T, class Cv>
-void run_solve(uchol_factor_s* F, int nrhs, Cv* work, Cv* fv) {
+template <class T, class Cv, int SB>
+void run_solve(uchol_factor_s* F, int nrhs, Cv* work, Cv* fv, Cv* fv2, cudaStream_t st) {
     uchol_symbolic_s* S = F->sym;
     DevPlan& D = *F->dp;
     const Plan& P = D.plan;
-    cudaStream_t st = S->stream;
     SolveArgs A;
     A.sn = D.sn.as<SnDev>();
     A.rel = D.rel.as<int>();
@@ -484,6 +540,7 @@ void run_solve(uchol_factor_s* F, int nrhs, Cv* work, Cv* fv) {
     A.nrhs = nrhs;
     A.ldw = S->n;
     const T* panel = F->panel.as<T>();
+    const Cv* linv = F->linv.as<Cv>();
     const int* fronts = D.solve_fronts.as<int>();
     const SolveBlockTask* tasks = D.solve_tasks.as<SolveBlockTask>();
     const double* diag = F->diag.as<double>();
@@ -491,26 +548,63 @@ void run_solve(uchol_factor_s* F, int nrhs, Cv* work, Cv* fv) {
         if (L.count == 0) continue;
         switch (L.kind) {
             case SolveLaunch::FwdGather: k_fwd_gather<Cv><<<L.count, 128, 0, st>>>(fronts + L.begin, A, work, fv); break;
-            case SolveLaunch::FwdDiag: k_fwd_diag<T, Cv><<<L.count, 64, 0, st>>>(tasks + L.begin, A, panel, fv); break;
-            case SolveLaunch::FwdRows: k_fwd_rows<T, Cv><<<L.count, 128, 0, st>>>(tasks + L.begin, A, panel, fv); break;
-            case SolveLaunch::FwdFinish: k_fwd_finish<Cv><<<L.count, 128, 0, st>>>(fronts + L.begin, A, diag, fv, work); break;
+            case SolveLaunch::FwdBlock:
+                k_fwd_block<T, Cv, SB><<<L.count, 128, 0, st>>>(tasks + L.begin, A, panel, linv, fv, fv2);
+                break;
+            case SolveLaunch::FwdFinish: k_fwd_finish<Cv><<<L.count, 128, 0, st>>>(fronts + L.begin, A, diag, fv2, work); break;
             default: break;
         }
-        counted();
     }
     for (const SolveLaunch& L : P.bwd_launches) {
         if (L.count == 0) continue;
         switch (L.kind) {
             case SolveLaunch::BwdGather: k_bwd_gather<Cv><<<L.count, 128, 0, st>>>(fronts + L.begin, A, work, fv); break;
-            case SolveLaunch::BwdTail:
-            case SolveLaunch::BwdCols: k_bwd_cols<T, Cv><<<L.count, 256, 0, st>>>(tasks + L.begin, A, panel, fv); break;
-            case SolveLaunch::BwdDiag: k_bwd_diag<T, Cv><<<L.count, 64, 0, st>>>(tasks + L.begin, A, panel, fv); break;
-            case SolveLaunch::BwdFinish: k_bwd_finish<Cv><<<L.count, 128, 0, st>>>(fronts + L.begin, A, fv, work); break;
+            case SolveLaunch::BwdTail: k_bwd_cols<T, Cv><<<L.count, 256, 0, st>>>(tasks + L.begin, A, panel, fv); break;
+            case SolveLaunch::BwdBlock:
+                k_bwd_block<T, Cv, SB><<<L.count, 256, 0, st>>>(tasks + L.begin, A, panel, linv, fv, fv2);
+                break;
+            case SolveLaunch::BwdFinish: k_bwd_finish<Cv><<<L.count, 128, 0, st>>>(fronts + L.begin, A, fv2, work); break;
             default: break;
         }
-        counted();
     }
     CK(cudaGetLastError());
+}
+
+int solve_launch_count(const Plan& P) {
+    int c = 0;
+    for (const SolveLaunch& L : P.fwd_launches) c += L.count > 0;
+    for (const SolveLaunch& L : P.bwd_launches) c += L.count > 0;
+    return c;
+}
+
+// The triangular solves of a factor for nrhs columns, captured once into a
+// CUDA graph over the factor's fixed work buffers and replayed on each call.
+template <class T, class Cv, int SB>
+void launch_solve_graph(uchol_factor_s* F, int nrhs, Cv* work, cudaStream_t st) {
+    if (!F->solve_graph || F->solve_graph_nrhs != nrhs) {
+        if (F->solve_graph) {
+            CK(cudaGraphExecDestroy(F->solve_graph));
+            F->solve_graph = nullptr;
+        }
+        if (!F->capture_stream) CK(cudaStreamCreateWithFlags(&F->capture_stream, cudaStreamNonBlocking));
+        cudaGraph_t g = nullptr;
+        CK(cudaStreamBeginCapture(F->capture_stream, cudaStreamCaptureModeThreadLocal));
+        try {
+            run_solve<T, Cv, SB>(F, nrhs, work, F->fv.as<Cv>(), F->fv2.as<Cv>(), F->capture_stream);
+        } catch (...) {
+            cudaStreamEndCapture(F->capture_stream, &g);
+            if (g) cudaGraphDestroy(g);
+            throw;
+        }
+        CK(cudaStreamEndCapture(F->capture_stream, &g));
+        cudaError_t e = cudaGraphInstantiate(&F->solve_graph, g, 0);
+        cudaGraphDestroy(g);
+        CK(e);
+        F->solve_graph_nrhs = nrhs;
+        F->solve_graph_nodes = solve_launch_count(F->dp->plan);
+    }
+    CK(cudaGraphLaunch(F->solve_graph, st));
+    counted(F->solve_graph_nodes);
 }
 
 void ensure_workspace(uchol_factor_s* F, int nrhs) {
@@ -520,6 +614,11 @@ void ensure_workspace(uchol_factor_s* F, int nrhs) {
     size_t cv = F->precision == UCHOL_PRECISION_FP64 ? 8 : 4;
     F->work.alloc((size_t)std::max(1, S->n) * nrhs * cv, "solve workspace");
     F->fv.alloc((size_t)P.fvec_elems * nrhs * cv, "solve workspace");
+    F->fv2.alloc((size_t)P.fvec_elems * nrhs * cv, "solve workspace");
+    if (F->solve_graph) {
+        CK(cudaGraphExecDestroy(F->solve_graph));
+        F->solve_graph = nullptr;
+    }
     for (auto& v : F->vec) v.alloc((size_t)std::max(1, S->n) * nrhs * sizeof(double), "refinement vectors");
     F->scal.alloc((size_t)(kDotBlocks * nrhs + 16 * nrhs) * sizeof(double), "refinement scalars");
     F->ws_nrhs = nrhs;
@@ -535,13 +634,13 @@ void apply_factor(uchol_factor_s* F, int nrhs, const double* b, int ldb, double*
     if (F->precision == UCHOL_PRECISION_FP64) {
         double* work = F->work.as<double>();
         k_permute_in<double><<<g, 256, 0, st>>>(b, ldb, S->d_perm.as<int>(), n, nrhs, work, n);
-        if (S->count) run_solve<double, double>(F, nrhs, work, F->fv.as<double>());
+        if (S->count) launch_solve_graph<double, double, 64>(F, nrhs, work, st);
         k_permute_out<double><<<g, 256, 0, st>>>(work, n, S->d_perm.as<int>(), n, nrhs, x, ldx);
         counted(2);
     } else {
         float* work = F->work.as<float>();
         k_permute_in<float><<<g, 256, 0, st>>>(b, ldb, S->d_perm.as<int>(), n, nrhs, work, n);
-        if (S->count) run_solve<float, float>(F, nrhs, work, F->fv.as<float>());
+        if (S->count) launch_solve_graph<float, float, 128>(F, nrhs, work, st);
         k_permute_out<float><<<g, 256, 0, st>>>(work, n, S->d_perm.as<int>(), n, nrhs, x, ldx);
         counted(2);
     }
@@ -792,7 +891,7 @@ int uchol_estimate_device_bytes(const uchol_symbolic_desc* d, const uchol_option
         const int64_t op = o.precision == UCHOL_PRECISION_BF16 ? 2 : 4;
         if (factor_bytes) *factor_bytes = P.factor_elems * elem;
         if (contribution_bytes) *contribution_bytes = P.contrib_elems * elem;
-        if (staging_bytes) *staging_bytes = cfg.tensor_core ? 2 * P.stage_rows * cfg.outer_block * op : 0;
+        if (staging_bytes) *staging_bytes = cfg.tensor_core ? 2 * P.stage_elems * op : 0;
         if (levels) *levels = P.levels;
         if (launches) *launches = (int)P.launches.size();
     });
@@ -862,7 +961,6 @@ int uchol_factor_destroy(uchol_factor f) {
     return guarded([&] {
         if (!f) return;
         cudaStreamSynchronize(f->sym->stream);
-        destroy_tc_maps(f->maps);
         delete f;
     });
 }

@@ -55,9 +55,18 @@ struct EaEntry {
 
 struct PanelTask {     // FP64 pivot block [j0, j0+nb) of front s plus TRSM of rows [row0, row0+rows)
     int s, j0, nb, row0, rows;
-    int stage_row;     // first staging row of this task's rows (-1: no staging)
-    int stage_k;       // K offset of column j0 inside the staging block
-    int stage_zero_to; // > 0: also clear staging columns [stage_k + nb, stage_zero_to)
+    int stage;         // 1: also write the K-major staging copies W = L D and L (tensor-core path)
+    int pad0;
+    int stage_zero_to; // > 0: also clear staging columns [j0 + nb, stage_zero_to) of these rows
+};
+
+// Staging region of a large front on the tensor-core path: m rows (front
+// rows) x ld K columns (the supernode's columns, ld = w rounded up to 64),
+// one region for W = L D (A operand) and one for L (B operand).
+struct StageInfo {
+    long long off;     // element offset of the front's region in each staging arena
+    int ld;
+    int map;           // index of the front's tensor-map pair
 };
 
 struct TileTask {      // C[i0:i0+TM, j0:j0+TN] -= sum_k A[i,k] B[j,k], k in [k0, k0+kn)

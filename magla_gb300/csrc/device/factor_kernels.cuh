@@ -229,7 +229,8 @@ __global__ void __launch_bounds__(128) k_pivot_block(const PanelTask* __restrict
 template <class T, class Op, class Cc, int NBMAX>
 __global__ void __launch_bounds__(128) k_trsm(const PanelTask* __restrict__ tasks, const SnDev* __restrict__ sn,
                                               T* __restrict__ panel, const double* __restrict__ diag,
-                                              Op* __restrict__ stage_a, Op* __restrict__ stage_b, int stage_ld) {
+                                              Op* __restrict__ stage_a, Op* __restrict__ stage_b,
+                                              const StageInfo* __restrict__ stage_info) {
     __shared__ Cc L11[NBMAX * (NBMAX + 1)];
     __shared__ double dpiv[NBMAX];
     __shared__ double dinv[NBMAX];
@@ -259,21 +260,24 @@ __global__ void __launch_bounds__(128) k_trsm(const PanelTask* __restrict__ task
                 y[k] = v;
             }
         }
+        long long so = 0;
+        if (tk.stage) {
+            const StageInfo g = stage_info[tk.s];
+            so = g.off + (long long)i * g.ld;
+        }
 #pragma unroll
         for (int k = 0; k < NBMAX; ++k) {
             if (k < nb) {
                 const double l = (double)y[k] * dinv[k];
                 P[i + (long long)(j0 + k) * d.ldp] = (T)l;
-                if (tk.stage_row >= 0) {
-                    const long long so = (long long)(tk.stage_row + tid) * stage_ld + tk.stage_k + k;
-                    stage_a[so] = (Op)(float)(l * dpiv[k]);
-                    stage_b[so] = (Op)(float)l;
+                if (tk.stage) {
+                    stage_a[so + j0 + k] = (Op)(float)(l * dpiv[k]);
+                    stage_b[so + j0 + k] = (Op)(float)l;
                 }
             }
         }
-        if (tk.stage_row >= 0 && tk.stage_zero_to > 0) {
-            const long long so = (long long)(tk.stage_row + tid) * stage_ld;
-            for (int k = tk.stage_k + nb; k < tk.stage_zero_to; ++k) {
+        if (tk.stage && tk.stage_zero_to > 0) {
+            for (int k = j0 + nb; k < tk.stage_zero_to; ++k) {
                 stage_a[so + k] = (Op)0.0f;
                 stage_b[so + k] = (Op)0.0f;
             }

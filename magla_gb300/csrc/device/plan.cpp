@@ -228,6 +228,7 @@ Plan build_plan(int n, int count, const int* first_column, const int* parent, co
     }
 
     // ---- factorisation launches, level by level ----
+    P.stage.assign(count, StageInfo{0, 0, -1});
     const int PB = cfg.pivot_block;
     const int NB = cfg.tensor_core ? cfg.outer_block : cfg.pivot_block;
     const int TS = cfg.tile;
@@ -287,23 +288,21 @@ Plan build_plan(int n, int count, const int* first_column, const int* parent, co
         // large fronts: blocked right-looking factorisation in lockstep
         int max_w = 0;
         for (int s : large) max_w = std::max(max_w, P.sn[s].w);
-        for (int k0 = 0; k0 < max_w; k0 += NB) {
-            // staging rows of this outer step (tensor-core operands of the trailing update)
-            std::map<int, long long> stage_base;
-            long long stage_top = 0;
-            if (cfg.tensor_core) {
-                for (int s : large) {
-                    const SnDev& d = P.sn[s];
-                    if (d.w <= k0) continue;
-                    int nbo = std::min(NB, d.w - k0);
-                    int rows = d.m - (k0 + nbo);
-                    if (rows > 0) {
-                        stage_base[s] = stage_top;
-                        stage_top += round_up(rows, 128);
-                    }
-                }
-                P.stage_rows = std::max(P.stage_rows, stage_top);
+        if (cfg.tensor_core) {
+            // one staging region per large front of the level (the arena is reused by every level)
+            long long top = 0;
+            for (int s : large) {
+                const SnDev& d = P.sn[s];
+                StageInfo& g = P.stage[s];
+                g.ld = (int)round_up(d.w, 64);
+                g.off = top;
+                g.map = (int)P.map_front.size();
+                P.map_front.push_back(s);
+                top += round_up((long long)d.m * g.ld, 256);
             }
+            P.stage_elems = std::max(P.stage_elems, top);
+        }
+        for (int k0 = 0; k0 < max_w; k0 += NB) {
             for (int j0r = 0; j0r < NB; j0r += PB) {
                 int qb = (int)P.pivot_tasks.size();
                 int pb = (int)P.panel_tasks.size();
@@ -318,17 +317,13 @@ Plan build_plan(int n, int count, const int* first_column, const int* parent, co
                     int nbi = std::min(PB, k0 + nbo - j0);
                     int outer_end = k0 + nbo;
                     P.pivot_tasks.push_back({s, j0, nbi, j0 + nbi, 0, -1, 0, 0});
-                    // TRSM tasks over rows [j0+nbi, m), broken at outer_end for staging
+                    // TRSM tasks over rows [j0+nbi, m)
                     int r = j0 + nbi;
                     while (r < d.m) {
-                        int lim = r < outer_end ? outer_end : d.m;
-                        int rows = std::min(128, lim - r);
-                        int srow = -1, zero_to = 0;
-                        if (cfg.tensor_core && r >= outer_end) {
-                            srow = (int)(stage_base[s] + (r - outer_end));
-                            if (j0 + nbi == outer_end && nbo < NB) zero_to = NB;
-                        }
-                        P.panel_tasks.push_back({s, j0, nbi, r, rows, srow, j0 - k0, zero_to});
+                        int rows = std::min(128, d.m - r);
+                        int stage = cfg.tensor_core ? 1 : 0, zero_to = 0;
+                        if (cfg.tensor_core && j0 + nbi == d.w && P.stage[s].ld > d.w) zero_to = P.stage[s].ld;
+                        P.panel_tasks.push_back({s, j0, nbi, r, rows, stage, 0, zero_to});
                         r += rows;
                     }
                     // inner update of the rest of the outer block (tensor-core configuration only)
@@ -345,11 +340,27 @@ Plan build_plan(int n, int count, const int* first_column, const int* parent, co
                     P.launches.push_back({Launch::SimtUpdate, ub, (int)P.simt_jobs.size() - ub, utiles});
                 if (!cfg.tensor_core) break;  // FP64 path: one pivot block per outer step
             }
-            // trailing update of the outer step
-            {
-                auto& jobs = cfg.tensor_core ? P.tc_jobs : P.simt_jobs;
-                const int T = cfg.tensor_core ? cfg.tc_tile_m : TS;
-                int jb = (int)jobs.size();
+            // trailing update of the outer step: the whole trailing triangle on the FP64
+            // path; only the supernode's remaining columns on the tensor-core path (the
+            // contribution block is updated once per front, after its last step)
+            if (cfg.tensor_core) {
+                int jb = (int)P.tc_jobs.size();
+                long long tiles = 0;
+                for (int s : large) {
+                    const SnDev& d = P.sn[s];
+                    if (d.w <= k0) continue;
+                    int nbo = std::min(NB, d.w - k0);
+                    int c0 = k0 + nbo;
+                    if (c0 >= d.w) continue;
+                    UpdJob U{tiles, s, c0, d.w, k0, nbo, -1};
+                    P.tc_jobs.push_back({tiles, s, c0, d.w, k0, nbo, P.stage[s].map});
+                    tiles += job_tiles(U, d, cfg.tc_tile_m);
+                    P.tc_flops += job_flops(U, d);
+                }
+                if ((int)P.tc_jobs.size() > jb)
+                    P.launches.push_back({Launch::TcUpdate, jb, (int)P.tc_jobs.size() - jb, tiles});
+            } else {
+                int jb = (int)P.simt_jobs.size();
                 long long tiles = 0;
                 for (int s : large) {
                     const SnDev& d = P.sn[s];
@@ -357,15 +368,28 @@ Plan build_plan(int n, int count, const int* first_column, const int* parent, co
                     int nbo = std::min(NB, d.w - k0);
                     int c0 = k0 + nbo;
                     if (c0 >= d.m) continue;
-                    UpdJob J{tiles, s, c0, d.m, k0, nbo, cfg.tensor_core ? (int)stage_base[s] : -1};
-                    tiles += job_tiles(J, d, T);
-                    (cfg.tensor_core ? P.tc_flops : P.simt_flops) += job_flops(J, d);
-                    jobs.push_back(J);
+                    UpdJob J{tiles, s, c0, d.m, k0, nbo, -1};
+                    tiles += job_tiles(J, d, TS);
+                    P.simt_flops += job_flops(J, d);
+                    P.simt_jobs.push_back(J);
                 }
-                if ((int)jobs.size() > jb)
-                    P.launches.push_back({cfg.tensor_core ? Launch::TcUpdate : Launch::SimtUpdate, jb,
-                                          (int)jobs.size() - jb, tiles});
+                if ((int)P.simt_jobs.size() > jb)
+                    P.launches.push_back({Launch::SimtUpdate, jb, (int)P.simt_jobs.size() - jb, tiles});
             }
+        }
+        // tensor-core path: contribution block of every large front, K = its whole width
+        if (cfg.tensor_core) {
+            int jb = (int)P.tc_jobs.size();
+            long long tiles = 0;
+            for (int s : large) {
+                const SnDev& d = P.sn[s];
+                if (d.m == d.w) continue;
+                UpdJob U{tiles, s, d.w, d.m, 0, d.w, -1};
+                P.tc_jobs.push_back({tiles, s, d.w, d.m, 0, d.w, P.stage[s].map});
+                tiles += job_tiles(U, d, cfg.tc_tile_m);
+                P.tc_flops += job_flops(U, d);
+            }
+            if ((int)P.tc_jobs.size() > jb) P.launches.push_back({Launch::TcUpdate, jb, (int)P.tc_jobs.size() - jb, tiles});
         }
     }
 
@@ -378,6 +402,14 @@ Plan build_plan(int n, int count, const int* first_column, const int* parent, co
     }
     P.fvec_elems = std::max<long long>(fo, 8);
     const int SB = cfg.solve_block;
+    // diagonal blocks of every supernode (inverted once per factorisation)
+    std::vector<int> first_blk(count, 0);
+    for (int s = 0; s < count; ++s) {
+        first_blk[s] = (int)P.inv_blocks.size();
+        for (int k0 = 0; k0 < P.sn[s].w; k0 += SB)
+            P.inv_blocks.push_back({s, k0, std::min(SB, P.sn[s].w - k0), 0, 0, 1, (int)P.inv_blocks.size()});
+    }
+    constexpr int kRowChunk = 128, kColChunk = 32;
     for (int L = 0; L < P.levels; ++L) {
         const auto& fronts = at_level[L];
         int fb = (int)P.solve_fronts.size();
@@ -387,34 +419,33 @@ Plan build_plan(int n, int count, const int* first_column, const int* parent, co
         int max_w = 0;
         for (int s : fronts) max_w = std::max(max_w, P.sn[s].w);
         for (int k0 = 0; k0 < max_w; k0 += SB) {
-            int db = (int)P.solve_tasks.size();
-            for (int s : fronts)
-                if (P.sn[s].w > k0) P.solve_tasks.push_back({s, k0, std::min(SB, P.sn[s].w - k0), 0, 0});
-            P.fwd_launches.push_back({SolveLaunch::FwdDiag, db, (int)P.solve_tasks.size() - db});
-            int rb = (int)P.solve_tasks.size();
+            int tb = (int)P.solve_tasks.size();
             for (int s : fronts) {
                 const SnDev& d = P.sn[s];
                 if (d.w <= k0) continue;
                 int kn = std::min(SB, d.w - k0);
-                for (int r = k0 + kn; r < d.m; r += 128)
-                    P.solve_tasks.push_back({s, k0, kn, r, std::min(d.m, r + 128)});
+                int blk = first_blk[s] + k0 / SB;
+                int r = k0 + kn;
+                if (r >= d.m) P.solve_tasks.push_back({s, k0, kn, r, r, 1, blk});
+                for (; r < d.m; r += kRowChunk)
+                    P.solve_tasks.push_back({s, k0, kn, r, std::min(d.m, r + kRowChunk), r == k0 + kn, blk});
             }
-            if ((int)P.solve_tasks.size() > rb) P.fwd_launches.push_back({SolveLaunch::FwdRows, rb, (int)P.solve_tasks.size() - rb});
+            P.fwd_launches.push_back({SolveLaunch::FwdBlock, tb, (int)P.solve_tasks.size() - tb});
         }
         P.fwd_launches.push_back({SolveLaunch::FwdFinish, fb, fcount});
     }
+    std::vector<int> level_begin(P.levels + 1, 0);
+    for (int L = 0; L < P.levels; ++L) level_begin[L + 1] = level_begin[L] + (int)at_level[L].size();
     for (int L = P.levels - 1; L >= 0; --L) {
         const auto& fronts = at_level[L];
-        // fronts of this level are already listed contiguously in solve_fronts; find them
-        int fb = 0;
-        for (int l = 0; l < L; ++l) fb += (int)at_level[l].size();
+        int fb = level_begin[L];
         int fcount = (int)fronts.size();
         P.bwd_launches.push_back({SolveLaunch::BwdGather, fb, fcount});
         int tb = (int)P.solve_tasks.size();
         for (int s : fronts) {
             const SnDev& d = P.sn[s];
             if (d.m == d.w) continue;
-            for (int c = 0; c < d.w; c += 8) P.solve_tasks.push_back({s, c, std::min(8, d.w - c), d.w, d.m});
+            for (int c = 0; c < d.w; c += 8) P.solve_tasks.push_back({s, c, std::min(8, d.w - c), d.w, d.m, 0, 0});
         }
         if ((int)P.solve_tasks.size() > tb) P.bwd_launches.push_back({SolveLaunch::BwdTail, tb, (int)P.solve_tasks.size() - tb});
         int max_w = 0;
@@ -422,19 +453,17 @@ Plan build_plan(int n, int count, const int* first_column, const int* parent, co
         int blocks = (max_w + SB - 1) / SB;
         for (int b = blocks - 1; b >= 0; --b) {
             int k0 = b * SB;
-            int db = (int)P.solve_tasks.size();
-            for (int s : fronts)
-                if (P.sn[s].w > k0) P.solve_tasks.push_back({s, k0, std::min(SB, P.sn[s].w - k0), 0, 0});
-            P.bwd_launches.push_back({SolveLaunch::BwdDiag, db, (int)P.solve_tasks.size() - db});
-            if (k0 == 0) continue;
-            int cb = (int)P.solve_tasks.size();
+            int tb2 = (int)P.solve_tasks.size();
             for (int s : fronts) {
                 const SnDev& d = P.sn[s];
                 if (d.w <= k0) continue;
                 int kn = std::min(SB, d.w - k0);
-                for (int c = 0; c < k0; c += 8) P.solve_tasks.push_back({s, c, std::min(8, k0 - c), k0, k0 + kn});
+                int blk = first_blk[s] + b;
+                if (k0 == 0) P.solve_tasks.push_back({s, k0, kn, 0, 0, 1, blk});
+                for (int c = 0; c < k0; c += kColChunk)
+                    P.solve_tasks.push_back({s, k0, kn, c, std::min(k0, c + kColChunk), c == 0, blk});
             }
-            if ((int)P.solve_tasks.size() > cb) P.bwd_launches.push_back({SolveLaunch::BwdCols, cb, (int)P.solve_tasks.size() - cb});
+            P.bwd_launches.push_back({SolveLaunch::BwdBlock, tb2, (int)P.solve_tasks.size() - tb2});
         }
         P.bwd_launches.push_back({SolveLaunch::BwdFinish, fb, fcount});
     }

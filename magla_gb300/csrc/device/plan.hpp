@@ -34,13 +34,23 @@ struct Launch {
 
 struct SolveLaunch {
     enum Kind : int {
-        FwdGather, FwdDiag, FwdRows, FwdFinish, BwdGather, BwdTail, BwdDiag, BwdCols, BwdFinish
+        FwdGather, FwdBlock, FwdFinish, BwdGather, BwdTail, BwdBlock, BwdFinish, Invert
     } kind;
     int begin, count;
 };
 
-struct SolveBlockTask {   // block [k0, k0+kn) of supernode s; rows [r0, r1) for row/column updates
+// Diagonal block [k0, k0+kn) of supernode s (its inverse is block `blk` of the
+// inverse arena); rows (forward) or columns (backward) [r0, r1) updated with it;
+// the leader task also stores the block's solution.
+struct SolveBlockTask {
     int s, k0, kn, r0, r1;
+    int leader, blk;
+};
+
+// Host mirror of the device TcJob (tc_gemm.cuh): one rank-kn update of a front.
+struct TcJobHost {
+    long long tile_begin;
+    int s, c0, cend, kbeg, kn, map;
 };
 
 struct Plan {
@@ -63,16 +73,19 @@ struct Plan {
     std::vector<PanelTask> pivot_tasks;   // one per (front, pivot block)
     std::vector<PanelTask> panel_tasks;   // TRSM row chunks
     std::vector<UpdJob> simt_jobs;
-    std::vector<UpdJob> tc_jobs;
+    std::vector<TcJobHost> tc_jobs;
+    std::vector<StageInfo> stage;              // per supernode (tensor-core path)
+    std::vector<int> map_front;                // front of each tensor-map pair
     std::vector<Launch> launches;
     int max_small_m = 0;
-    long long stage_rows = 0;                  // rows of the operand staging arena (tensor-core path)
+    long long stage_elems = 0;                 // elements of each operand staging arena (tensor-core path)
     double tc_flops = 0.0;                     // algorithmic flops of the tensor-core updates (lower triangle)
     double simt_flops = 0.0;                   // algorithmic flops of the SIMT updates
 
     // solve tasks
     std::vector<int> solve_fronts;             // supernode lists for gather/finish launches
     std::vector<SolveBlockTask> solve_tasks;
+    std::vector<SolveBlockTask> inv_blocks;    // every diagonal block, for the inversion after a factorisation
     std::vector<SolveLaunch> fwd_launches, bwd_launches;
 };
 

@@ -16,6 +16,8 @@
 
 namespace uchol_dev {
 
+__device__ __forceinline__ SolveBlockTask blocks_or_tasks(const SolveBlockTask* __restrict__ t) { return t[blockIdx.x]; }
+
 struct SolveArgs {
     const SnDev* sn;
     const int* rel;
@@ -65,54 +67,111 @@ __global__ void k_fwd_gather(const int* __restrict__ fronts, SolveArgs A, const 
     }
 }
 
-// Unit lower triangular solve with the diagonal block [k0, k0+kn).
-template <class T, class Cv>
-__global__ void k_fwd_diag(const SolveBlockTask* __restrict__ tasks, SolveArgs A, const T* __restrict__ panel,
-                           Cv* __restrict__ fv) {
-    __shared__ Cv Lb[64 * 65];
-    __shared__ Cv x[64];
-    const SolveBlockTask tk = tasks[blockIdx.x];
-    const SnDev d = A.sn[tk.s];
+// Inverse of every unit-lower diagonal block (SB x SB, column-major), one
+// CTA per block, thread c computing column c by forward substitution.
+template <class T, class Cv, int SB>
+__global__ void __launch_bounds__(SB) k_invert_blocks(const SolveBlockTask* __restrict__ blocks, const SnDev* __restrict__ sn,
+                                                      const T* __restrict__ panel, Cv* __restrict__ linv) {
+    extern __shared__ unsigned char inv_smem[];
+    Cv* Lb = reinterpret_cast<Cv*>(inv_smem);
+    Cv* X = Lb + SB * SB;
+    const SolveBlockTask tk = blocks[blockIdx.x];
+    const SnDev d = sn[tk.s];
     const T* P = panel + d.panel_off;
     const int kn = tk.kn;
     for (int idx = threadIdx.x; idx < kn * kn; idx += blockDim.x) {
         int r = idx % kn, c = idx / kn;
-        Lb[r + c * 65] = r > c ? (Cv)P[(tk.k0 + r) + (long long)(tk.k0 + c) * d.ldp] : Cv(0);
+        Lb[r + c * SB] = r > c ? (Cv)P[(tk.k0 + r) + (long long)(tk.k0 + c) * d.ldp] : Cv(0);
     }
-    for (int r = 0; r < A.nrhs; ++r) {
-        Cv* f = fv + A.fvec_off[tk.s] + r * A.fv_stride + tk.k0;
-        __syncthreads();
-        if (threadIdx.x < kn) x[threadIdx.x] = f[threadIdx.x];
-        __syncthreads();
-        for (int k = 0; k < kn - 1; ++k) {
-            const Cv xk = x[k];
-            __syncthreads();
-            int i = threadIdx.x;
-            if (i > k && i < kn) x[i] -= Lb[i + k * 65] * xk;
-            __syncthreads();
+    __syncthreads();
+    const int c = threadIdx.x;
+    if (c < kn) {
+        for (int r = 0; r < kn; ++r) {
+            Cv v = r == c ? Cv(1) : Cv(0);
+            if (r > c)
+                for (int k = c; k < r; ++k) v -= Lb[r + k * SB] * X[k + c * SB];
+            X[r + c * SB] = v;
         }
-        if (threadIdx.x < kn) f[threadIdx.x] = x[threadIdx.x];
+    }
+    __syncthreads();
+    Cv* out = linv + (long long)tk.blk * SB * SB;
+    for (int idx = threadIdx.x; idx < SB * SB; idx += blockDim.x) {
+        int r = idx % SB, cc = idx / SB;
+        out[idx] = (r < kn && cc < kn) ? X[r + cc * SB] : Cv(0);
     }
 }
 
-// f[i] -= sum_{k in block} L[i,k] f[k] for rows [r0, r1).
-template <class T, class Cv>
-__global__ void k_fwd_rows(const SolveBlockTask* __restrict__ tasks, SolveArgs A, const T* __restrict__ panel,
-                           Cv* __restrict__ fv) {
-    __shared__ Cv xb[64];
-    const SolveBlockTask tk = tasks[blockIdx.x];
+// Forward step of one diagonal block: y = L11^-1 f[block] from the stored
+// inverse (every task recomputes it), the leader stores y, and the task's
+// rows below are updated: f[i] -= L[i, block] y.
+template <class T, class Cv, int SB>
+__global__ void __launch_bounds__(128) k_fwd_block(const SolveBlockTask* __restrict__ tasks, SolveArgs A,
+                                                   const T* __restrict__ panel, const Cv* __restrict__ linv,
+                                                   Cv* __restrict__ fv, Cv* __restrict__ yv) {
+    __shared__ Cv fb[SB];
+    __shared__ Cv y[SB];
+    const SolveBlockTask tk = blocks_or_tasks(tasks);
     const SnDev d = A.sn[tk.s];
     const T* P = panel + d.panel_off;
-    const int i = tk.r0 + threadIdx.x;
+    const Cv* Li = linv + (long long)tk.blk * SB * SB;
+    const int kn = tk.kn;
     for (int r = 0; r < A.nrhs; ++r) {
-        Cv* f = fv + A.fvec_off[tk.s] + r * A.fv_stride;
+        const long long base = A.fvec_off[tk.s] + r * A.fv_stride;
+        Cv* f = fv + base;
         __syncthreads();
-        if (threadIdx.x < tk.kn) xb[threadIdx.x] = f[tk.k0 + threadIdx.x];
+        for (int t = threadIdx.x; t < kn; t += blockDim.x) fb[t] = f[tk.k0 + t];
         __syncthreads();
-        if (i < tk.r1) {
+        for (int t = threadIdx.x; t < kn; t += blockDim.x) {
             Cv acc = Cv(0);
-            for (int k = 0; k < tk.kn; ++k) acc += (Cv)P[i + (long long)(tk.k0 + k) * d.ldp] * xb[k];
+            for (int k = 0; k <= t; ++k) acc += Li[t + k * SB] * fb[k];
+            y[t] = acc;
+        }
+        __syncthreads();
+        if (tk.leader)
+            for (int t = threadIdx.x; t < kn; t += blockDim.x) yv[base + tk.k0 + t] = y[t];
+        for (int i = tk.r0 + threadIdx.x; i < tk.r1; i += blockDim.x) {
+            Cv acc = Cv(0);
+            for (int k = 0; k < kn; ++k) acc += (Cv)P[i + (long long)(tk.k0 + k) * d.ldp] * y[k];
             f[i] -= acc;
+        }
+    }
+}
+
+// Backward step of one diagonal block: x = L11^-T g[block] (every task
+// recomputes it), the leader stores x, and the task's columns c < k0 are
+// updated: g[c] -= L[block, c]^T x (one warp per column).
+template <class T, class Cv, int SB>
+__global__ void __launch_bounds__(256) k_bwd_block(const SolveBlockTask* __restrict__ tasks, SolveArgs A,
+                                                   const T* __restrict__ panel, const Cv* __restrict__ linv,
+                                                   Cv* __restrict__ fv, Cv* __restrict__ xv) {
+    __shared__ Cv gb[SB];
+    __shared__ Cv x[SB];
+    const SolveBlockTask tk = blocks_or_tasks(tasks);
+    const SnDev d = A.sn[tk.s];
+    const T* P = panel + d.panel_off;
+    const Cv* Li = linv + (long long)tk.blk * SB * SB;
+    const int kn = tk.kn;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int r = 0; r < A.nrhs; ++r) {
+        const long long base = A.fvec_off[tk.s] + r * A.fv_stride;
+        Cv* g = fv + base;
+        __syncthreads();
+        for (int t = threadIdx.x; t < kn; t += blockDim.x) gb[t] = g[tk.k0 + t];
+        __syncthreads();
+        for (int t = threadIdx.x; t < kn; t += blockDim.x) {
+            Cv acc = Cv(0);
+            for (int k = t; k < kn; ++k) acc += Li[k + t * SB] * gb[k];
+            x[t] = acc;
+        }
+        __syncthreads();
+        if (tk.leader)
+            for (int t = threadIdx.x; t < kn; t += blockDim.x) xv[base + tk.k0 + t] = x[t];
+        for (int c = tk.r0 + warp; c < tk.r1; c += 8) {
+            const T* col = P + (long long)c * d.ldp + tk.k0;
+            Cv acc = Cv(0);
+            for (int i = lane; i < kn; i += 32) acc += (Cv)col[i] * x[i];
+            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            if (lane == 0) g[c] -= acc;
         }
     }
 }
@@ -158,36 +217,6 @@ __global__ void k_bwd_cols(const SolveBlockTask* __restrict__ tasks, SolveArgs A
         for (int i = tk.r0 + lane; i < tk.r1; i += 32) acc += (Cv)col[i] * g[i];
         for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
         if (lane == 0) g[k] -= acc;
-    }
-}
-
-// Unit upper solve with the transposed diagonal block [k0, k0+kn).
-template <class T, class Cv>
-__global__ void k_bwd_diag(const SolveBlockTask* __restrict__ tasks, SolveArgs A, const T* __restrict__ panel,
-                           Cv* __restrict__ fv) {
-    __shared__ Cv Lb[64 * 65];
-    __shared__ Cv x[64];
-    const SolveBlockTask tk = tasks[blockIdx.x];
-    const SnDev d = A.sn[tk.s];
-    const T* P = panel + d.panel_off;
-    const int kn = tk.kn;
-    for (int idx = threadIdx.x; idx < kn * kn; idx += blockDim.x) {
-        int r = idx % kn, c = idx / kn;
-        Lb[r + c * 65] = r > c ? (Cv)P[(tk.k0 + r) + (long long)(tk.k0 + c) * d.ldp] : Cv(0);
-    }
-    for (int r = 0; r < A.nrhs; ++r) {
-        Cv* g = fv + A.fvec_off[tk.s] + r * A.fv_stride + tk.k0;
-        __syncthreads();
-        if (threadIdx.x < kn) x[threadIdx.x] = g[threadIdx.x];
-        __syncthreads();
-        for (int k = kn - 1; k > 0; --k) {
-            const Cv xk = x[k];
-            __syncthreads();
-            int j = threadIdx.x;
-            if (j < k) x[j] -= Lb[k + j * 65] * xk;
-            __syncthreads();
-        }
-        if (threadIdx.x < kn) g[threadIdx.x] = x[threadIdx.x];
     }
 }
 
