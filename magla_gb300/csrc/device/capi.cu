@@ -290,19 +290,22 @@ void run_factor_launches(uchol_factor_s* F, cudaStream_t st) {
                 break;
             case Launch::Trsm: {
                 const PanelTask* tk = D.panel_tasks.as<PanelTask>() + L.begin;
-                if (F->precision == UCHOL_PRECISION_BF16)
-                    k_trsm<T, __nv_bfloat16, float, 32><<<L.count, 128, 0, st>>>(
-                        tk, sn, panel, diag, F->stage_a.as<__nv_bfloat16>(), F->stage_b.as<__nv_bfloat16>(),
-                        D.stage.as<StageInfo>());
-                else if (F->precision == UCHOL_PRECISION_TF32)
-                    k_trsm<T, float, float, 32><<<L.count, 128, 0, st>>>(tk, sn, panel, diag, F->stage_a.as<float>(),
-                                                                          F->stage_b.as<float>(), D.stage.as<StageInfo>());
-                else if (P.cfg.pivot_block <= 32)
-                    k_trsm<T, T, double, 32><<<L.count, 128, 0, st>>>(tk, sn, panel, diag, nullptr, nullptr,
-                                                                       D.stage.as<StageInfo>());
-                else
-                    k_trsm<T, T, double, 64><<<L.count, 128, 0, st>>>(tk, sn, panel, diag, nullptr, nullptr,
-                                                                       D.stage.as<StageInfo>());
+                if constexpr (sizeof(T) == 4) {
+                    if (F->precision == UCHOL_PRECISION_BF16)
+                        k_trsm<T, __nv_bfloat16, float, 32><<<L.count, 128, 0, st>>>(
+                            tk, sn, panel, diag, F->stage_a.as<__nv_bfloat16>(), F->stage_b.as<__nv_bfloat16>(),
+                            D.stage.as<StageInfo>());
+                    else
+                        k_trsm<T, float, float, 32><<<L.count, 128, 0, st>>>(
+                            tk, sn, panel, diag, F->stage_a.as<float>(), F->stage_b.as<float>(), D.stage.as<StageInfo>());
+                } else {
+                    if (P.cfg.pivot_block <= 32)
+                        k_trsm<T, T, double, 32><<<L.count, 128, 0, st>>>(tk, sn, panel, diag, nullptr, nullptr,
+                                                                           D.stage.as<StageInfo>());
+                    else
+                        k_trsm<T, T, double, 64><<<L.count, 128, 0, st>>>(tk, sn, panel, diag, nullptr, nullptr,
+                                                                           D.stage.as<StageInfo>());
+                }
                 break;
             }
             case Launch::SimtUpdate:
@@ -541,29 +544,36 @@ void run_solve(uchol_factor_s* F, int nrhs, Cv* work, Cv* fv, Cv* fv2, cudaStrea
     A.ldw = S->n;
     const T* panel = F->panel.as<T>();
     const Cv* linv = F->linv.as<Cv>();
-    const int* fronts = D.solve_fronts.as<int>();
     const SolveBlockTask* tasks = D.solve_tasks.as<SolveBlockTask>();
     const double* diag = F->diag.as<double>();
     for (const SolveLaunch& L : P.fwd_launches) {
         if (L.count == 0) continue;
         switch (L.kind) {
-            case SolveLaunch::FwdGather: k_fwd_gather<Cv><<<L.count, 128, 0, st>>>(fronts + L.begin, A, work, fv); break;
-            case SolveLaunch::FwdBlock:
-                k_fwd_block<T, Cv, SB><<<L.count, 128, 0, st>>>(tasks + L.begin, A, panel, linv, fv, fv2);
+            case SolveLaunch::FwdGather: k_fwd_gather<Cv><<<L.count, 256, 0, st>>>(tasks + L.begin, A, work, fv); break;
+            case SolveLaunch::FwdStart:
+                k_block_start<Cv, SB, true><<<L.count, 256, SB * SB * sizeof(Cv), st>>>(tasks + L.begin, A, linv, fv, fv2);
                 break;
-            case SolveLaunch::FwdFinish: k_fwd_finish<Cv><<<L.count, 128, 0, st>>>(fronts + L.begin, A, diag, fv2, work); break;
+            case SolveLaunch::FwdBlock:
+                k_fwd_block<T, Cv, SB><<<L.count, 128, SB * SB * sizeof(Cv), st>>>(tasks + L.begin, A, panel, linv, fv,
+                                                                                   fv2);
+                break;
+            case SolveLaunch::FwdFinish: k_fwd_finish<Cv><<<L.count, 256, 0, st>>>(tasks + L.begin, A, diag, fv2, work); break;
             default: break;
         }
     }
     for (const SolveLaunch& L : P.bwd_launches) {
         if (L.count == 0) continue;
         switch (L.kind) {
-            case SolveLaunch::BwdGather: k_bwd_gather<Cv><<<L.count, 128, 0, st>>>(fronts + L.begin, A, work, fv); break;
+            case SolveLaunch::BwdGather: k_bwd_gather<Cv><<<L.count, 256, 0, st>>>(tasks + L.begin, A, work, fv); break;
             case SolveLaunch::BwdTail: k_bwd_cols<T, Cv><<<L.count, 256, 0, st>>>(tasks + L.begin, A, panel, fv); break;
-            case SolveLaunch::BwdBlock:
-                k_bwd_block<T, Cv, SB><<<L.count, 256, 0, st>>>(tasks + L.begin, A, panel, linv, fv, fv2);
+            case SolveLaunch::BwdStart:
+                k_block_start<Cv, SB, false><<<L.count, 256, SB * SB * sizeof(Cv), st>>>(tasks + L.begin, A, linv, fv, fv2);
                 break;
-            case SolveLaunch::BwdFinish: k_bwd_finish<Cv><<<L.count, 128, 0, st>>>(fronts + L.begin, A, fv2, work); break;
+            case SolveLaunch::BwdBlock:
+                k_bwd_block<T, Cv, SB><<<L.count, 256, SB * SB * sizeof(Cv), st>>>(tasks + L.begin, A, panel, linv, fv,
+                                                                                   fv2);
+                break;
+            case SolveLaunch::BwdFinish: k_bwd_finish<Cv><<<L.count, 256, 0, st>>>(tasks + L.begin, A, fv2, work); break;
             default: break;
         }
     }
@@ -587,6 +597,14 @@ void launch_solve_graph(uchol_factor_s* F, int nrhs, Cv* work, cudaStream_t st) 
             F->solve_graph = nullptr;
         }
         if (!F->capture_stream) CK(cudaStreamCreateWithFlags(&F->capture_stream, cudaStreamNonBlocking));
+        CK(cudaFuncSetAttribute(k_fwd_block<T, Cv, SB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)(SB * SB * sizeof(Cv))));
+        CK(cudaFuncSetAttribute(k_bwd_block<T, Cv, SB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)(SB * SB * sizeof(Cv))));
+        CK(cudaFuncSetAttribute(k_block_start<Cv, SB, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)(SB * SB * sizeof(Cv))));
+        CK(cudaFuncSetAttribute(k_block_start<Cv, SB, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)(SB * SB * sizeof(Cv))));
         cudaGraph_t g = nullptr;
         CK(cudaStreamBeginCapture(F->capture_stream, cudaStreamCaptureModeThreadLocal));
         try {

@@ -120,7 +120,22 @@ __global__ void k_extend_add(const EaItem* __restrict__ items, int count, const 
         const int t = C.m - C.w;
         const int* r = rel + C.rel_off;
         const T* src = contrib + C.contrib_off + (long long)en.a * C.ldc;
-        for (int b = en.a + lane; b < t; b += 32) dst[r[b] - shift] += src[b];
+        // rows of one child column are distinct, so loads of a batch are issued before its stores
+        for (int b0 = en.a + lane; b0 < t; b0 += 32 * 4) {
+            int idx[4];
+            T sv[4], dv[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int b = b0 + 32 * u;
+                idx[u] = b < t ? r[b] - shift : -1;
+                sv[u] = b < t ? src[b] : T(0);
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) dv[u] = idx[u] >= 0 ? dst[idx[u]] : T(0);
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (idx[u] >= 0) dst[idx[u]] = dv[u] + sv[u];
+        }
         __syncwarp();
     }
 }
@@ -234,6 +249,11 @@ __global__ void __launch_bounds__(128) k_trsm(const PanelTask* __restrict__ task
     __shared__ Cc L11[NBMAX * (NBMAX + 1)];
     __shared__ double dpiv[NBMAX];
     __shared__ double dinv[NBMAX];
+    // staging rows of this task, transposed for coalesced stores (only the
+    // tensor-core path stages: its operand types are at most 4 bytes)
+    constexpr int kStageRows = sizeof(Op) <= 4 ? 128 : 1;
+    __shared__ Op sa[kStageRows * (NBMAX + 1)];
+    __shared__ Op sb[kStageRows * (NBMAX + 1)];
     const PanelTask tk = tasks[blockIdx.x];
     const SnDev d = sn[tk.s];
     const int nb = tk.nb, j0 = tk.j0, ld = NBMAX + 1;
@@ -260,27 +280,32 @@ __global__ void __launch_bounds__(128) k_trsm(const PanelTask* __restrict__ task
                 y[k] = v;
             }
         }
-        long long so = 0;
-        if (tk.stage) {
-            const StageInfo g = stage_info[tk.s];
-            so = g.off + (long long)i * g.ld;
-        }
 #pragma unroll
         for (int k = 0; k < NBMAX; ++k) {
             if (k < nb) {
                 const double l = (double)y[k] * dinv[k];
                 P[i + (long long)(j0 + k) * d.ldp] = (T)l;
-                if (tk.stage) {
-                    stage_a[so + j0 + k] = (Op)(float)(l * dpiv[k]);
-                    stage_b[so + j0 + k] = (Op)(float)l;
+                if (kStageRows > 1 && tk.stage) {
+                    sa[tid * ld + k] = (Op)(float)(l * dpiv[k]);
+                    sb[tid * ld + k] = (Op)(float)l;
                 }
             }
         }
-        if (tk.stage && tk.stage_zero_to > 0) {
-            for (int k = j0 + nb; k < tk.stage_zero_to; ++k) {
-                stage_a[so + k] = (Op)0.0f;
-                stage_b[so + k] = (Op)0.0f;
-            }
+    }
+    if (kStageRows == 1 || !tk.stage) return;
+    __syncthreads();
+    // one warp per row: lanes store consecutive K columns of the row
+    const StageInfo g = stage_info[tk.s];
+    const int warp = tid >> 5, lane = tid & 31;
+    for (int r = warp; r < tk.rows; r += nt >> 5) {
+        const long long so = g.off + (long long)(tk.row0 + r) * g.ld;
+        for (int k = lane; k < nb; k += 32) {
+            stage_a[so + j0 + k] = sa[r * ld + k];
+            stage_b[so + j0 + k] = sb[r * ld + k];
+        }
+        for (int k = j0 + nb + lane; k < tk.stage_zero_to; k += 32) {
+            stage_a[so + k] = (Op)0.0f;
+            stage_b[so + k] = (Op)0.0f;
         }
     }
 }

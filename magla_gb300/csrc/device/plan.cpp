@@ -303,6 +303,22 @@ Plan build_plan(int n, int count, const int* first_column, const int* parent, co
             P.stage_elems = std::max(P.stage_elems, top);
         }
         for (int k0 = 0; k0 < max_w; k0 += NB) {
+            // tensor-core path: left-looking update of the outer block [k0, k0+NB) with every
+            // earlier column of its supernode (K = k0), read once and written once
+            if (cfg.tensor_core && k0 > 0) {
+                int jb = (int)P.tc_jobs.size();
+                long long tiles = 0;
+                for (int s : large) {
+                    const SnDev& d = P.sn[s];
+                    if (d.w <= k0) continue;
+                    int nbo = std::min(NB, d.w - k0);
+                    UpdJob U{tiles, s, k0, k0 + nbo, 0, k0, -1};
+                    P.tc_jobs.push_back({tiles, s, k0, k0 + nbo, 0, k0, P.stage[s].map});
+                    tiles += job_tiles(U, d, cfg.tc_tile_m);
+                    P.tc_flops += job_flops(U, d);
+                }
+                if ((int)P.tc_jobs.size() > jb) P.launches.push_back({Launch::TcUpdate, jb, (int)P.tc_jobs.size() - jb, tiles});
+            }
             for (int j0r = 0; j0r < NB; j0r += PB) {
                 int qb = (int)P.pivot_tasks.size();
                 int pb = (int)P.panel_tasks.size();
@@ -340,26 +356,8 @@ Plan build_plan(int n, int count, const int* first_column, const int* parent, co
                     P.launches.push_back({Launch::SimtUpdate, ub, (int)P.simt_jobs.size() - ub, utiles});
                 if (!cfg.tensor_core) break;  // FP64 path: one pivot block per outer step
             }
-            // trailing update of the outer step: the whole trailing triangle on the FP64
-            // path; only the supernode's remaining columns on the tensor-core path (the
-            // contribution block is updated once per front, after its last step)
-            if (cfg.tensor_core) {
-                int jb = (int)P.tc_jobs.size();
-                long long tiles = 0;
-                for (int s : large) {
-                    const SnDev& d = P.sn[s];
-                    if (d.w <= k0) continue;
-                    int nbo = std::min(NB, d.w - k0);
-                    int c0 = k0 + nbo;
-                    if (c0 >= d.w) continue;
-                    UpdJob U{tiles, s, c0, d.w, k0, nbo, -1};
-                    P.tc_jobs.push_back({tiles, s, c0, d.w, k0, nbo, P.stage[s].map});
-                    tiles += job_tiles(U, d, cfg.tc_tile_m);
-                    P.tc_flops += job_flops(U, d);
-                }
-                if ((int)P.tc_jobs.size() > jb)
-                    P.launches.push_back({Launch::TcUpdate, jb, (int)P.tc_jobs.size() - jb, tiles});
-            } else {
+            // FP64 path: right-looking update of the whole trailing triangle per step
+            if (!cfg.tensor_core) {
                 int jb = (int)P.simt_jobs.size();
                 long long tiles = 0;
                 for (int s : large) {
@@ -409,13 +407,29 @@ Plan build_plan(int n, int count, const int* first_column, const int* parent, co
         for (int k0 = 0; k0 < P.sn[s].w; k0 += SB)
             P.inv_blocks.push_back({s, k0, std::min(SB, P.sn[s].w - k0), 0, 0, 1, (int)P.inv_blocks.size()});
     }
-    constexpr int kRowChunk = 128, kColChunk = 32;
+    const int kRowChunk = SB, kColChunk = SB;
+    constexpr int kGatherChunk = 2048;
+    // chunked per-front tasks: rows [r0, r1) of the front vector (gathers) or
+    // own columns [r0, r1) (finishes)
+    auto chunk_tasks = [&](const std::vector<int>& fronts, bool own_columns) {
+        int b = (int)P.solve_tasks.size();
+        for (int s : fronts) {
+            const int lim = own_columns ? P.sn[s].w : P.sn[s].m;
+            for (int r = 0; r < lim; r += kGatherChunk)
+                P.solve_tasks.push_back({s, 0, 0, r, std::min(lim, r + kGatherChunk), 0, 0});
+        }
+        return std::make_pair(b, (int)P.solve_tasks.size() - b);
+    };
     for (int L = 0; L < P.levels; ++L) {
         const auto& fronts = at_level[L];
-        int fb = (int)P.solve_fronts.size();
-        P.solve_fronts.insert(P.solve_fronts.end(), fronts.begin(), fronts.end());
-        int fcount = (int)fronts.size();
-        P.fwd_launches.push_back({SolveLaunch::FwdGather, fb, fcount});
+        {
+            auto g = chunk_tasks(fronts, false);
+            P.fwd_launches.push_back({SolveLaunch::FwdGather, g.first, g.second});
+            int sb = (int)P.solve_tasks.size();
+            for (int s : fronts)
+                P.solve_tasks.push_back({s, 0, std::min(SB, P.sn[s].w), 0, 0, 0, first_blk[s]});
+            P.fwd_launches.push_back({SolveLaunch::FwdStart, sb, (int)P.solve_tasks.size() - sb});
+        }
         int max_w = 0;
         for (int s : fronts) max_w = std::max(max_w, P.sn[s].w);
         for (int k0 = 0; k0 < max_w; k0 += SB) {
@@ -425,22 +439,24 @@ Plan build_plan(int n, int count, const int* first_column, const int* parent, co
                 if (d.w <= k0) continue;
                 int kn = std::min(SB, d.w - k0);
                 int blk = first_blk[s] + k0 / SB;
-                int r = k0 + kn;
-                if (r >= d.m) P.solve_tasks.push_back({s, k0, kn, r, r, 1, blk});
-                for (; r < d.m; r += kRowChunk)
-                    P.solve_tasks.push_back({s, k0, kn, r, std::min(d.m, r + kRowChunk), r == k0 + kn, blk});
+                for (int r = k0 + kn; r < d.m; r += kRowChunk) {
+                    const int fl = (r == k0 + kn && r < d.w) ? kSolveNext : 0;   // rows [r, r+SB) are the next block
+                    P.solve_tasks.push_back({s, k0, kn, r, std::min(d.m, r + kRowChunk), fl, blk});
+                }
             }
             P.fwd_launches.push_back({SolveLaunch::FwdBlock, tb, (int)P.solve_tasks.size() - tb});
         }
-        P.fwd_launches.push_back({SolveLaunch::FwdFinish, fb, fcount});
+        {
+            auto g = chunk_tasks(fronts, true);
+            P.fwd_launches.push_back({SolveLaunch::FwdFinish, g.first, g.second});
+        }
     }
-    std::vector<int> level_begin(P.levels + 1, 0);
-    for (int L = 0; L < P.levels; ++L) level_begin[L + 1] = level_begin[L] + (int)at_level[L].size();
     for (int L = P.levels - 1; L >= 0; --L) {
         const auto& fronts = at_level[L];
-        int fb = level_begin[L];
-        int fcount = (int)fronts.size();
-        P.bwd_launches.push_back({SolveLaunch::BwdGather, fb, fcount});
+        {
+            auto g = chunk_tasks(fronts, false);
+            P.bwd_launches.push_back({SolveLaunch::BwdGather, g.first, g.second});
+        }
         int tb = (int)P.solve_tasks.size();
         for (int s : fronts) {
             const SnDev& d = P.sn[s];
@@ -448,6 +464,15 @@ Plan build_plan(int n, int count, const int* first_column, const int* parent, co
             for (int c = 0; c < d.w; c += 8) P.solve_tasks.push_back({s, c, std::min(8, d.w - c), d.w, d.m, 0, 0});
         }
         if ((int)P.solve_tasks.size() > tb) P.bwd_launches.push_back({SolveLaunch::BwdTail, tb, (int)P.solve_tasks.size() - tb});
+        {
+            int sb = (int)P.solve_tasks.size();
+            for (int s : fronts) {
+                const int nbk = (P.sn[s].w + SB - 1) / SB;
+                const int k0 = (nbk - 1) * SB;
+                P.solve_tasks.push_back({s, k0, P.sn[s].w - k0, 0, 0, 0, first_blk[s] + nbk - 1});
+            }
+            P.bwd_launches.push_back({SolveLaunch::BwdStart, sb, (int)P.solve_tasks.size() - sb});
+        }
         int max_w = 0;
         for (int s : fronts) max_w = std::max(max_w, P.sn[s].w);
         int blocks = (max_w + SB - 1) / SB;
@@ -459,13 +484,16 @@ Plan build_plan(int n, int count, const int* first_column, const int* parent, co
                 if (d.w <= k0) continue;
                 int kn = std::min(SB, d.w - k0);
                 int blk = first_blk[s] + b;
-                if (k0 == 0) P.solve_tasks.push_back({s, k0, kn, 0, 0, 1, blk});
-                for (int c = 0; c < k0; c += kColChunk)
-                    P.solve_tasks.push_back({s, k0, kn, c, std::min(k0, c + kColChunk), c == 0, blk});
+                // column chunks aligned to the blocks: the chunk [k0 - SB, k0) is the previous block
+                for (int c = k0 - SB; c >= 0; c -= kColChunk)
+                    P.solve_tasks.push_back({s, k0, kn, c, c + kColChunk, c == k0 - SB ? kSolveNext : 0, blk});
             }
             P.bwd_launches.push_back({SolveLaunch::BwdBlock, tb2, (int)P.solve_tasks.size() - tb2});
         }
-        P.bwd_launches.push_back({SolveLaunch::BwdFinish, fb, fcount});
+        {
+            auto g = chunk_tasks(fronts, true);
+            P.bwd_launches.push_back({SolveLaunch::BwdFinish, g.first, g.second});
+        }
     }
     return P;
 }

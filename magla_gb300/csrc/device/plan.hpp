@@ -34,17 +34,19 @@ struct Launch {
 
 struct SolveLaunch {
     enum Kind : int {
-        FwdGather, FwdBlock, FwdFinish, BwdGather, BwdTail, BwdBlock, BwdFinish, Invert
+        FwdGather, FwdStart, FwdBlock, FwdFinish, BwdGather, BwdTail, BwdStart, BwdBlock, BwdFinish
     } kind;
     int begin, count;
 };
 
 // Diagonal block [k0, k0+kn) of supernode s (its inverse is block `blk` of the
-// inverse arena); rows (forward) or columns (backward) [r0, r1) updated with it;
-// the leader task also stores the block's solution.
+// inverse arena); rows (forward) or columns (backward) [r0, r1) updated with
+// the block's solution.  Flag kSolveNext: this task's rows (columns) are the
+// next block; after the update it computes and stores that block's solution.
+constexpr int kSolveNext = 4;
 struct SolveBlockTask {
     int s, k0, kn, r0, r1;
-    int leader, blk;
+    int flags, blk;
 };
 
 // Host mirror of the device TcJob (tc_gemm.cuh): one rank-kn update of a front.

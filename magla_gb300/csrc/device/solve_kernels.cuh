@@ -45,23 +45,48 @@ __global__ void k_permute_out(const Cv* __restrict__ work, int ldw, const int* _
             x[perm[i] + (long long)r * ldx] = (double)work[i + (long long)r * ldw];
 }
 
+// Rows [r0, r1) of a front vector: the supernode's right-hand side (own
+// columns) plus, child by child, the child's update vector entries that map
+// into these rows (relative indices are sorted, so each child contributes a
+// contiguous range found by binary search).
+__device__ __forceinline__ int lower_bound_int(const int* a, int n, int key) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (a[mid] < key) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
 template <class Cv>
-__global__ void k_fwd_gather(const int* __restrict__ fronts, SolveArgs A, const Cv* __restrict__ work,
+__global__ void k_fwd_gather(const SolveBlockTask* __restrict__ tasks, SolveArgs A, const Cv* __restrict__ work,
                              Cv* __restrict__ fv) {
-    const int s = fronts[blockIdx.x];
+    __shared__ int range[2];
+    const SolveBlockTask tk = tasks[blockIdx.x];
+    const int s = tk.s;
     const SnDev d = A.sn[s];
     for (int r = 0; r < A.nrhs; ++r) {
         Cv* f = fv + A.fvec_off[s] + r * A.fv_stride;
-        for (int a = threadIdx.x; a < d.m; a += blockDim.x)
+        for (int a = tk.r0 + threadIdx.x; a < tk.r1; a += blockDim.x)
             f[a] = a < d.w ? work[d.first_col + a + (long long)r * A.ldw] : Cv(0);
         __syncthreads();
         for (int c = A.child_ptr[s]; c < A.child_ptr[s + 1]; ++c) {
             const int ch = A.children[c];
             const SnDev cd = A.sn[ch];
             const int t = cd.m - cd.w;
-            const Cv* u = fv + A.fvec_off[ch] + r * A.fv_stride + cd.w;
             const int* rl = A.rel + cd.rel_off;
-            for (int b = threadIdx.x; b < t; b += blockDim.x) f[rl[b]] += u[b];
+            if (tk.r0 == 0 && tk.r1 == d.m) {   // the chunk is the whole front
+                if (threadIdx.x == 0) {
+                    range[0] = 0;
+                    range[1] = t;
+                }
+            } else if (threadIdx.x == 0) {
+                range[0] = lower_bound_int(rl, t, tk.r0);
+                range[1] = lower_bound_int(rl, t, tk.r1);
+            }
+            __syncthreads();
+            const Cv* u = fv + A.fvec_off[ch] + r * A.fv_stride + cd.w;
+            for (int b = range[0] + threadIdx.x; b < range[1]; b += blockDim.x) f[rl[b]] += u[b];
             __syncthreads();
         }
     }
@@ -101,103 +126,205 @@ __global__ void __launch_bounds__(SB) k_invert_blocks(const SolveBlockTask* __re
     }
 }
 
-// Forward step of one diagonal block: y = L11^-1 f[block] from the stored
-// inverse (every task recomputes it), the leader stores y, and the task's
-// rows below are updated: f[i] -= L[i, block] y.
-template <class T, class Cv, int SB>
-__global__ void __launch_bounds__(128) k_fwd_block(const SolveBlockTask* __restrict__ tasks, SolveArgs A,
-                                                   const T* __restrict__ panel, const Cv* __restrict__ linv,
-                                                   Cv* __restrict__ fv, Cv* __restrict__ yv) {
-    __shared__ Cv fb[SB];
-    __shared__ Cv y[SB];
-    const SolveBlockTask tk = blocks_or_tasks(tasks);
-    const SnDev d = A.sn[tk.s];
-    const T* P = panel + d.panel_off;
-    const Cv* Li = linv + (long long)tk.blk * SB * SB;
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((unsigned)__cvta_generic_to_shared(smem)),
+                 "l"(gmem)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;" ::: "memory");
+}
+
+// Starts copying inverse block `src` (SB x SB) into shared memory.
+template <class Cv, int SB>
+__device__ __forceinline__ void prefetch_inverse(Cv* dst, const Cv* src) {
+    constexpr int chunks = SB * SB * (int)sizeof(Cv) / 16;
+    for (int q = threadIdx.x; q < chunks; q += blockDim.x) cp_async16(reinterpret_cast<char*>(dst) + 16 * q,
+                                                                       reinterpret_cast<const char*>(src) + 16 * q);
+}
+
+// First block solution of each front: forward y_0 = L_00^-1 f_0 (after the
+// gather), backward x_last = L_ll^-T g_last (after the trailing-row dots).
+template <class Cv, int SB, bool FORWARD>
+__global__ void __launch_bounds__(256) k_block_start(const SolveBlockTask* __restrict__ tasks, SolveArgs A,
+                                                     const Cv* __restrict__ linv, const Cv* __restrict__ fv,
+                                                     Cv* __restrict__ sol) {
+    extern __shared__ __align__(16) unsigned char blk_smem[];
+    Cv* Ls = reinterpret_cast<Cv*>(blk_smem);
+    __shared__ Cv v[SB];
+    const SolveBlockTask tk = tasks[blockIdx.x];
     const int kn = tk.kn;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+    prefetch_inverse<Cv, SB>(Ls, linv + (long long)tk.blk * SB * SB);
+    cp_async_wait_all();
     for (int r = 0; r < A.nrhs; ++r) {
         const long long base = A.fvec_off[tk.s] + r * A.fv_stride;
-        Cv* f = fv + base;
         __syncthreads();
-        for (int t = threadIdx.x; t < kn; t += blockDim.x) fb[t] = f[tk.k0 + t];
+        for (int t = threadIdx.x; t < kn; t += blockDim.x) v[t] = fv[base + tk.k0 + t];
         __syncthreads();
-        for (int t = threadIdx.x; t < kn; t += blockDim.x) {
-            Cv acc = Cv(0);
-            for (int k = 0; k <= t; ++k) acc += Li[t + k * SB] * fb[k];
-            y[t] = acc;
-        }
-        __syncthreads();
-        if (tk.leader)
-            for (int t = threadIdx.x; t < kn; t += blockDim.x) yv[base + tk.k0 + t] = y[t];
-        for (int i = tk.r0 + threadIdx.x; i < tk.r1; i += blockDim.x) {
-            Cv acc = Cv(0);
-            for (int k = 0; k < kn; ++k) acc += (Cv)P[i + (long long)(tk.k0 + k) * d.ldp] * y[k];
-            f[i] -= acc;
+        if (FORWARD) {
+            // thread per output row: consecutive threads read consecutive words of each inverse column
+            for (int t = threadIdx.x; t < kn; t += blockDim.x) {
+                Cv acc = Cv(0);
+                for (int k = 0; k <= t; ++k) acc += Ls[t + k * SB] * v[k];
+                sol[base + tk.k0 + t] = acc;
+            }
+        } else {
+            // warp per output: lanes read consecutive words of one inverse column
+            for (int t = warp; t < kn; t += nwarps) {
+                Cv acc = Cv(0);
+                for (int k = t + lane; k < kn; k += 32) acc += Ls[k + t * SB] * v[k];
+                for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+                if (lane == 0) sol[base + tk.k0 + t] = acc;
+            }
         }
     }
 }
 
-// Backward step of one diagonal block: x = L11^-T g[block] (every task
-// recomputes it), the leader stores x, and the task's columns c < k0 are
-// updated: g[c] -= L[block, c]^T x (one warp per column).
+// Forward step of diagonal block b of a front: y_b (in the solution buffer)
+// updates the task's rows, f[i] -= L[i, b] y_b.  The task whose rows are
+// block b+1 then computes y_{b+1} from their final values with the inverse
+// it prefetched at the start.
+template <class T, class Cv, int SB>
+__global__ void __launch_bounds__(128) k_fwd_block(const SolveBlockTask* __restrict__ tasks, SolveArgs A,
+                                                   const T* __restrict__ panel, const Cv* __restrict__ linv,
+                                                   Cv* __restrict__ fv, Cv* __restrict__ yv) {
+    extern __shared__ __align__(16) unsigned char blk_smem[];
+    Cv* Ls = reinterpret_cast<Cv*>(blk_smem);
+    __shared__ Cv y[SB];
+    __shared__ Cv fn[SB];
+    const SolveBlockTask tk = blocks_or_tasks(tasks);
+    const SnDev d = A.sn[tk.s];
+    const T* P = panel + d.panel_off;
+    const int kn = tk.kn;
+    const bool next = tk.flags & kSolveNext;
+    const int kn_next = next ? min(SB, d.w - (tk.k0 + kn)) : 0;
+    if (next) prefetch_inverse<Cv, SB>(Ls, linv + (long long)(tk.blk + 1) * SB * SB);
+    for (int r = 0; r < A.nrhs; ++r) {
+        const long long base = A.fvec_off[tk.s] + r * A.fv_stride;
+        Cv* f = fv + base;
+        __syncthreads();
+        for (int t = threadIdx.x; t < kn; t += blockDim.x) y[t] = yv[base + tk.k0 + t];
+        __syncthreads();
+        const int i = tk.r0 + threadIdx.x;
+        if (i < tk.r1) {
+            const T* row = P + i + (long long)tk.k0 * d.ldp;
+            Cv acc[4] = {Cv(0), Cv(0), Cv(0), Cv(0)};
+            int k = 0;
+            for (; k + 32 <= kn; k += 32) {
+                T vv[32];
+#pragma unroll
+                for (int u = 0; u < 32; ++u) vv[u] = row[(long long)(k + u) * d.ldp];
+#pragma unroll
+                for (int u = 0; u < 32; ++u) acc[u & 3] += (Cv)vv[u] * y[k + u];
+            }
+            for (; k < kn; ++k) acc[0] += (Cv)row[(long long)k * d.ldp] * y[k];
+            const Cv nv = f[i] - ((acc[0] + acc[1]) + (acc[2] + acc[3]));
+            f[i] = nv;
+            if (next && threadIdx.x < kn_next) fn[threadIdx.x] = nv;
+        }
+        if (next) {
+            if (r == 0) cp_async_wait_all();
+            __syncthreads();
+            for (int t = threadIdx.x; t < kn_next; t += blockDim.x) {
+                Cv acc = Cv(0);
+                for (int k = 0; k <= t; ++k) acc += Ls[t + k * SB] * fn[k];
+                yv[base + tk.k0 + kn + t] = acc;
+            }
+        }
+    }
+}
+
+// Backward step of diagonal block b of a front: x_b (in the solution buffer)
+// updates the task's columns c < k0, g[c] -= L[b, c]^T x_b (warp-cooperative
+// dots, four columns per warp pass).  The task whose columns are block b-1
+// then computes x_{b-1}.
 template <class T, class Cv, int SB>
 __global__ void __launch_bounds__(256) k_bwd_block(const SolveBlockTask* __restrict__ tasks, SolveArgs A,
                                                    const T* __restrict__ panel, const Cv* __restrict__ linv,
                                                    Cv* __restrict__ fv, Cv* __restrict__ xv) {
-    __shared__ Cv gb[SB];
+    extern __shared__ __align__(16) unsigned char blk_smem[];
+    Cv* Ls = reinterpret_cast<Cv*>(blk_smem);
     __shared__ Cv x[SB];
+    __shared__ Cv gn[SB];
     const SolveBlockTask tk = blocks_or_tasks(tasks);
     const SnDev d = A.sn[tk.s];
     const T* P = panel + d.panel_off;
-    const Cv* Li = linv + (long long)tk.blk * SB * SB;
     const int kn = tk.kn;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+    const bool next = tk.flags & kSolveNext;
+    if (next) prefetch_inverse<Cv, SB>(Ls, linv + (long long)(tk.blk - 1) * SB * SB);
     for (int r = 0; r < A.nrhs; ++r) {
         const long long base = A.fvec_off[tk.s] + r * A.fv_stride;
         Cv* g = fv + base;
         __syncthreads();
-        for (int t = threadIdx.x; t < kn; t += blockDim.x) gb[t] = g[tk.k0 + t];
+        for (int t = threadIdx.x; t < kn; t += blockDim.x) x[t] = xv[base + tk.k0 + t];
         __syncthreads();
-        for (int t = threadIdx.x; t < kn; t += blockDim.x) {
-            Cv acc = Cv(0);
-            for (int k = t; k < kn; ++k) acc += Li[k + t * SB] * gb[k];
-            x[t] = acc;
+        for (int c0 = tk.r0 + 4 * warp; c0 < tk.r1; c0 += 4 * nwarps) {
+            Cv acc[4] = {Cv(0), Cv(0), Cv(0), Cv(0)};
+            T vv[4][SB / 32];
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+#pragma unroll
+                for (int u = 0; u < SB / 32; ++u) {
+                    const int i = lane + 32 * u;
+                    vv[q][u] = (c0 + q < tk.r1 && i < kn) ? P[(long long)(c0 + q) * d.ldp + tk.k0 + i] : T(0);
+                }
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+#pragma unroll
+                for (int u = 0; u < SB / 32; ++u) {
+                    const int i = lane + 32 * u;
+                    if (i < kn) acc[q] += (Cv)vv[q][u] * x[i];
+                }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                Cv a = acc[q];
+                for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+                if (lane == 0 && c0 + q < tk.r1) {
+                    const Cv nv = g[c0 + q] - a;
+                    g[c0 + q] = nv;
+                    if (next) gn[c0 + q - tk.r0] = nv;
+                }
+            }
         }
-        __syncthreads();
-        if (tk.leader)
-            for (int t = threadIdx.x; t < kn; t += blockDim.x) xv[base + tk.k0 + t] = x[t];
-        for (int c = tk.r0 + warp; c < tk.r1; c += 8) {
-            const T* col = P + (long long)c * d.ldp + tk.k0;
-            Cv acc = Cv(0);
-            for (int i = lane; i < kn; i += 32) acc += (Cv)col[i] * x[i];
-            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-            if (lane == 0) g[c] -= acc;
+        if (next) {
+            if (r == 0) cp_async_wait_all();
+            __syncthreads();
+            for (int t = warp; t < SB; t += nwarps) {   // the previous block is always full width
+                Cv acc = Cv(0);
+                for (int k = t + lane; k < SB; k += 32) acc += Ls[k + t * SB] * gn[k];
+                for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+                if (lane == 0) xv[base + tk.r0 + t] = acc;
+            }
         }
     }
 }
 
 // y = f / D for the supernode's own columns (the diagonal step of the solve).
 template <class Cv>
-__global__ void k_fwd_finish(const int* __restrict__ fronts, SolveArgs A, const double* __restrict__ diag,
+__global__ void k_fwd_finish(const SolveBlockTask* __restrict__ tasks, SolveArgs A, const double* __restrict__ diag,
                              const Cv* __restrict__ fv, Cv* __restrict__ work) {
-    const int s = fronts[blockIdx.x];
+    const SolveBlockTask tk = tasks[blockIdx.x];
+    const int s = tk.s;
     const SnDev d = A.sn[s];
     for (int r = 0; r < A.nrhs; ++r) {
         const Cv* f = fv + A.fvec_off[s] + r * A.fv_stride;
-        for (int a = threadIdx.x; a < d.w; a += blockDim.x)
+        for (int a = tk.r0 + threadIdx.x; a < tk.r1; a += blockDim.x)
             work[d.first_col + a + (long long)r * A.ldw] = (Cv)((double)f[a] / diag[d.first_col + a]);
     }
 }
 
 template <class Cv>
-__global__ void k_bwd_gather(const int* __restrict__ fronts, SolveArgs A, const Cv* __restrict__ work,
+__global__ void k_bwd_gather(const SolveBlockTask* __restrict__ tasks, SolveArgs A, const Cv* __restrict__ work,
                              Cv* __restrict__ fv) {
-    const int s = fronts[blockIdx.x];
+    const SolveBlockTask tk = tasks[blockIdx.x];
+    const int s = tk.s;
     const SnDev d = A.sn[s];
     const int* rows = A.rows + d.rows_off;
     for (int r = 0; r < A.nrhs; ++r) {
         Cv* g = fv + A.fvec_off[s] + r * A.fv_stride;
-        for (int a = threadIdx.x; a < d.m; a += blockDim.x) g[a] = work[rows[a] + (long long)r * A.ldw];
+        for (int a = tk.r0 + threadIdx.x; a < tk.r1; a += blockDim.x) g[a] = work[rows[a] + (long long)r * A.ldw];
     }
 }
 
@@ -221,13 +348,14 @@ __global__ void k_bwd_cols(const SolveBlockTask* __restrict__ tasks, SolveArgs A
 }
 
 template <class Cv>
-__global__ void k_bwd_finish(const int* __restrict__ fronts, SolveArgs A, const Cv* __restrict__ fv,
+__global__ void k_bwd_finish(const SolveBlockTask* __restrict__ tasks, SolveArgs A, const Cv* __restrict__ fv,
                              Cv* __restrict__ work) {
-    const int s = fronts[blockIdx.x];
+    const SolveBlockTask tk = tasks[blockIdx.x];
+    const int s = tk.s;
     const SnDev d = A.sn[s];
     for (int r = 0; r < A.nrhs; ++r) {
         const Cv* g = fv + A.fvec_off[s] + r * A.fv_stride;
-        for (int a = threadIdx.x; a < d.w; a += blockDim.x) work[d.first_col + a + (long long)r * A.ldw] = g[a];
+        for (int a = tk.r0 + threadIdx.x; a < tk.r1; a += blockDim.x) work[d.first_col + a + (long long)r * A.ldw] = g[a];
     }
 }
 
