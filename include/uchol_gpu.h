@@ -87,9 +87,9 @@ typedef struct {
     int allow_diagonal_regularization;  /* AllowDiagonalRegularization (default 1) */
     double pivot_tolerance;             /* PivotTolerance (default 1e-13) */
     double diagonal_regularization;     /* DiagonalRegularization (default 1e-10) */
-    int panel_width;                    /* PanelWidth, clamped to 4..128: FP64 pivot-block width */
+    int panel_width;                    /* PanelWidth, clamped to 4..64: pivot-block width of the FP64 path */
     int precision;                      /* UCHOL_PRECISION_* */
-    int block_width;                    /* outer block of the tensor-core Schur GEMM (0 = tuned) */
+    int block_width;                    /* mixed paths: outer block, 64 or 128 columns (0 = 128) */
 } uchol_options;
 
 /* Pivot statistics (UtduNumericFactorization.cs:57-84) and timings. */

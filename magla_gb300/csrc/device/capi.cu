@@ -9,6 +9,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <type_traits>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -18,6 +19,7 @@
 
 #include "../../../include/uchol_gpu.h"
 #include "factor_kernels.cuh"
+#include "panel_kernels.cuh"
 #include "plan.hpp"
 #include "solve_kernels.cuh"
 #include "tc_gemm.cuh"
@@ -33,7 +35,8 @@ inline void counted(int k = 1) { g_launches += k; }
 inline bool phase_timing() {
     int v = g_phase_timing.load();
     if (v < 0) {
-        v = getenv("UCHOL_PHASE_TIMES") != nullptr ? 1 : 0;
+        const char* e = getenv("UCHOL_PHASE_TIMES");
+        v = (e && *e && strcmp(e, "0") != 0) ? 1 : 0;
         g_phase_timing.store(v);
     }
     return v != 0;
@@ -181,12 +184,16 @@ struct uchol_factor_s {
     DBuf panel, contrib, stage_a, stage_b, diag, values, full_val, stats, ctl;
     DBuf work, fv, fv2, vec[6], scal;   // solve workspace
     DBuf linv;                          // inverses of the diagonal blocks (solves)
+    DBuf minv;                          // mixed path: per outer block X^T, D, D^{-1} of each diagonal block
     int ws_nrhs = 0;
     cudaStream_t capture_stream = nullptr;
     cudaGraphExec_t solve_graph = nullptr;
     int solve_graph_nrhs = 0, solve_graph_nodes = 0;
+    cudaGraphExec_t factor_graph = nullptr;
+    int factor_graph_nodes = 0;
     ~uchol_factor_s() {
         if (solve_graph) cudaGraphExecDestroy(solve_graph);
+        if (factor_graph) cudaGraphExecDestroy(factor_graph);
         if (capture_stream) cudaStreamDestroy(capture_stream);
     }
     DBuf maps;                    // tensor-map pairs of the staging regions
@@ -230,13 +237,9 @@ PlanConfig config_for(const uchol_options& o) {
         c.solve_block = 128;
         c.tensor_core = true;
         c.pivot_block = std::min(c.pivot_block, 32);
-        int nb = o.block_width > 0 ? o.block_width : 128;
-        // whole-K staging in shared memory: at most 4 blocks of 128 bytes per operand row
-        const int nb_max = o.precision == UCHOL_PRECISION_BF16 ? 256 : 128;
-        nb = std::max(64, std::min(nb_max, nb / 64 * 64));
-        // the outer block must be a multiple of the pivot block
-        nb = nb / c.pivot_block * c.pivot_block;
-        c.outer_block = nb;
+        // outer block: 64 or 128 columns (the diagonal-block kernel holds at most kDiagMax)
+        int nb = o.block_width > 0 ? o.block_width : kDiagMax;
+        c.outer_block = std::max(64, std::min(kDiagMax, nb / 64 * 64));
     }
     return c;
 }
@@ -256,9 +259,7 @@ void run_factor_launches(uchol_factor_s* F, cudaStream_t st) {
     const bool timing = phase_timing();
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev;
     std::vector<int> ev_kind;
-    size_t small_smem = (size_t)P.max_small_m * P.max_small_m * sizeof(double);
-    if (small_smem > 48 * 1024)
-        CK(cudaFuncSetAttribute(k_small_fronts<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)small_smem));
+    const size_t small_smem = (size_t)P.max_small_m * P.max_small_m * sizeof(double);
     for (const Launch& L : P.launches) {
         if (timing) {
             cudaEvent_t a, b;
@@ -285,37 +286,46 @@ void run_factor_launches(uchol_factor_s* F, cudaStream_t st) {
                                                                     diag, ctl, stats);
                 break;
             case Launch::PivotBlock:
-                k_pivot_block<T><<<L.count, 128, 0, st>>>(D.pivot_tasks.as<PanelTask>() + L.begin, sn, panel, diag, ctl,
-                                                          stats);
-                break;
-            case Launch::Trsm: {
-                const PanelTask* tk = D.panel_tasks.as<PanelTask>() + L.begin;
-                if constexpr (sizeof(T) == 4) {
-                    if (F->precision == UCHOL_PRECISION_BF16)
-                        k_trsm<T, __nv_bfloat16, float, 32><<<L.count, 128, 0, st>>>(
-                            tk, sn, panel, diag, F->stage_a.as<__nv_bfloat16>(), F->stage_b.as<__nv_bfloat16>(),
-                            D.stage.as<StageInfo>());
+            case Launch::Trsm:
+            case Launch::SimtUpdate:
+                // FP64 path: 32- or 64-column pivot blocks, TRSM and right-looking updates in FP64
+                if constexpr (sizeof(T) == 8) {
+                    const PanelTask* pt = D.pivot_tasks.as<PanelTask>() + L.begin;
+                    const PanelTask* tk = D.panel_tasks.as<PanelTask>() + L.begin;
+                    if (L.kind == Launch::PivotBlock)
+                        k_pivot_block<T><<<L.count, 128, 0, st>>>(pt, sn, panel, diag, ctl, stats);
+                    else if (L.kind == Launch::SimtUpdate)
+                        k_simt_update<T, double><<<(unsigned)L.tiles, 256, 0, st>>>(
+                            D.simt_jobs.as<UpdJob>() + L.begin, L.count, sn, panel, contrib, diag);
+                    else if (P.cfg.pivot_block <= 32)
+                        k_trsm<T, double, 32><<<L.count, 128, 0, st>>>(tk, sn, panel, diag);
                     else
-                        k_trsm<T, float, float, 32><<<L.count, 128, 0, st>>>(
-                            tk, sn, panel, diag, F->stage_a.as<float>(), F->stage_b.as<float>(), D.stage.as<StageInfo>());
+                        k_trsm<T, double, 64><<<L.count, 128, 0, st>>>(tk, sn, panel, diag);
                 } else {
-                    if (P.cfg.pivot_block <= 32)
-                        k_trsm<T, T, double, 32><<<L.count, 128, 0, st>>>(tk, sn, panel, diag, nullptr, nullptr,
-                                                                           D.stage.as<StageInfo>());
-                    else
-                        k_trsm<T, T, double, 64><<<L.count, 128, 0, st>>>(tk, sn, panel, diag, nullptr, nullptr,
-                                                                           D.stage.as<StageInfo>());
+                    throw Error(UCHOL_INTERNAL, "FP64 panel launch in a mixed-precision plan");
                 }
                 break;
-            }
-            case Launch::SimtUpdate:
-                if (sizeof(T) == 8)
-                    k_simt_update<T, double><<<(unsigned)L.tiles, 256, 0, st>>>(D.simt_jobs.as<UpdJob>() + L.begin,
-                                                                                L.count, sn, panel, contrib, diag);
-                else
-                    k_simt_update<T, float><<<(unsigned)L.tiles, 256, 0, st>>>(D.simt_jobs.as<UpdJob>() + L.begin,
-                                                                               L.count, sn, panel, contrib, diag);
+            case Launch::DiagBlock:
+            case Launch::PanelSolve:
+                // mixed path: diagonal block, then its rows below as a GEMM with the block's inverse
+                if constexpr (sizeof(T) == 4) {
+                    if (L.kind == Launch::DiagBlock)
+                        k_diag_block<<<L.count, 256, kDiagSmemBytes, st>>>(D.pivot_tasks.as<PanelTask>() + L.begin, sn,
+                                                                           panel, diag, F->minv.as<float>(), ctl, stats);
+                    else if (F->precision == UCHOL_PRECISION_BF16)
+                        k_panel_solve<__nv_bfloat16><<<L.count, 256, 0, st>>>(
+                            D.panel_tasks.as<PanelTask>() + L.begin, sn, panel, F->minv.as<float>(),
+                            F->stage_a.as<__nv_bfloat16>(), F->stage_b.as<__nv_bfloat16>(), D.stage.as<StageInfo>());
+                    else
+                        k_panel_solve<float><<<L.count, 256, 0, st>>>(
+                            D.panel_tasks.as<PanelTask>() + L.begin, sn, panel, F->minv.as<float>(),
+                            F->stage_a.as<float>(), F->stage_b.as<float>(), D.stage.as<StageInfo>());
+                } else {
+                    throw Error(UCHOL_INTERNAL, "mixed-precision panel launch in an FP64 plan");
+                }
                 break;
+            case Launch::KindCount:
+                throw Error(UCHOL_INTERNAL, "invalid launch kind");
             case Launch::TcUpdate:
                 launch_tc_gemm(F->precision == UCHOL_PRECISION_BF16, D.tc_jobs.as<TcJob>() + L.begin, L.count, L.tiles,
                                sn, (float*)panel, (float*)contrib, F->maps.as<CUtensorMap>(), &stats->status, F->sms, st);
@@ -332,7 +342,7 @@ void run_factor_launches(uchol_factor_s* F, cudaStream_t st) {
     for (const Launch& L : P.launches) F->phases.schur_tensor_launches += L.kind == Launch::TcUpdate;
     if (timing) {
         CK(cudaStreamSynchronize(st));
-        double sum[8] = {0};
+        double sum[Launch::KindCount] = {0};
         for (size_t q = 0; q < ev.size(); ++q) {
             float ms = 0.f;
             CK(cudaEventElapsedTime(&ms, ev[q].first, ev[q].second));
@@ -342,10 +352,29 @@ void run_factor_launches(uchol_factor_s* F, cudaStream_t st) {
         }
         F->phases.extend_add_ms = sum[Launch::ExtendAdd] + sum[Launch::ZeroContrib];
         F->phases.small_fronts_ms = sum[Launch::SmallFronts];
-        F->phases.panel_ms = sum[Launch::PivotBlock] + sum[Launch::Trsm];
+        F->phases.panel_ms = sum[Launch::PivotBlock] + sum[Launch::Trsm] + sum[Launch::DiagBlock] + sum[Launch::PanelSolve];
         F->phases.schur_ms = sum[Launch::SimtUpdate] + sum[Launch::TcUpdate];
-        F->phases.pivot_block_ms = sum[Launch::PivotBlock];
+        F->phases.pivot_block_ms = sum[Launch::PivotBlock] + sum[Launch::DiagBlock];
         F->phases.schur_tensor_ms = sum[Launch::TcUpdate];
+    }
+}
+
+// Raises the dynamic shared-memory limits of every kernel a factorisation of
+// this configuration launches (done once, before any stream capture).
+void prepare_factor_kernels(uchol_factor_s* F) {
+    const Plan& P = F->dp->plan;
+    const int small = (int)((size_t)P.max_small_m * P.max_small_m * sizeof(double));
+    if (F->elem == 8) {
+        CK(cudaFuncSetAttribute(k_small_fronts<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, std::max(small, 1)));
+        CK(cudaFuncSetAttribute(k_invert_blocks<double, double, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)(2 * 64 * 64 * sizeof(double))));
+    } else {
+        CK(cudaFuncSetAttribute(k_small_fronts<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, std::max(small, 1)));
+        CK(cudaFuncSetAttribute(k_invert_blocks<float, float, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)(2 * 128 * 128 * sizeof(float))));
+        CK(cudaFuncSetAttribute(k_diag_block, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDiagSmemBytes));
+        CK(cudaFuncSetAttribute(k_tc_gemm<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_smem_bytes()));
+        CK(cudaFuncSetAttribute(k_tc_gemm<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_smem_bytes()));
     }
 }
 
@@ -359,13 +388,11 @@ void invert_diagonal_blocks(uchol_factor_s* F, cudaStream_t st) {
     if (F->elem == 8) {
         constexpr int SB = 64;
         const size_t smem = 2 * SB * SB * sizeof(double);
-        CK(cudaFuncSetAttribute(k_invert_blocks<double, double, SB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         k_invert_blocks<double, double, SB><<<nb, SB, smem, st>>>(D.inv_blocks.as<SolveBlockTask>(), D.sn.as<SnDev>(),
                                                                   F->panel.as<double>(), F->linv.as<double>());
     } else {
         constexpr int SB = 128;
         const size_t smem = 2 * SB * SB * sizeof(float);
-        CK(cudaFuncSetAttribute(k_invert_blocks<float, float, SB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         k_invert_blocks<float, float, SB><<<nb, SB, smem, st>>>(D.inv_blocks.as<SolveBlockTask>(), D.sn.as<SnDev>(),
                                                                 F->panel.as<float>(), F->linv.as<float>());
     }
@@ -402,15 +429,11 @@ void build_full_csr(uchol_symbolic_s* S) {
     S->d_full_src.upload(fsrc, S->stream, "product structure");
 }
 
-void factorize_impl(uchol_factor_s* F, const double* values, bool on_device) {
+// Every device operation of one numeric factorisation after the values are
+// in place: statistics reset, diagonal scale, product values, assembly,
+// the planned launches and the inverses of the diagonal blocks.
+void enqueue_factorization(uchol_factor_s* F, cudaStream_t st) {
     uchol_symbolic_s* S = F->sym;
-    cudaStream_t st = S->stream;
-    const Plan& P = F->dp->plan;
-    StreamTimer total(st);
-    if (on_device)
-        CK(cudaMemcpyAsync(F->values.p, values, (size_t)S->nnz * sizeof(double), cudaMemcpyDeviceToDevice, st));
-    else
-        CK(cudaMemcpyAsync(F->values.p, values, (size_t)S->nnz * sizeof(double), cudaMemcpyHostToDevice, st));
     PivotStats* stats = F->stats.as<PivotStats>();
     CK(cudaMemsetAsync(stats, 0, sizeof(PivotStats), st));
     if (S->n > 0) {
@@ -436,6 +459,45 @@ void factorize_impl(uchol_factor_s* F, const double* values, bool on_device) {
         if (F->elem == 8) run_factor_launches<double>(F, st);
         else run_factor_launches<float>(F, st);
         invert_diagonal_blocks(F, st);
+    }
+}
+
+void factorize_impl(uchol_factor_s* F, const double* values, bool on_device) {
+    uchol_symbolic_s* S = F->sym;
+    cudaStream_t st = S->stream;
+    const Plan& P = F->dp->plan;
+    StreamTimer total(st);
+    if (on_device)
+        CK(cudaMemcpyAsync(F->values.p, values, (size_t)S->nnz * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    else
+        CK(cudaMemcpyAsync(F->values.p, values, (size_t)S->nnz * sizeof(double), cudaMemcpyHostToDevice, st));
+    PivotStats* stats = F->stats.as<PivotStats>();
+    if (phase_timing()) {
+        enqueue_factorization(F, st);   // direct launches, one event pair each
+    } else {
+        // the whole launch sequence is captured once per factor and replayed:
+        // refactorisations with the same pattern cost one graph launch
+        if (!F->factor_graph) {
+            if (!F->capture_stream) CK(cudaStreamCreateWithFlags(&F->capture_stream, cudaStreamNonBlocking));
+            cudaGraph_t g = nullptr;
+            const long long before = g_launches.load();
+            CK(cudaStreamBeginCapture(F->capture_stream, cudaStreamCaptureModeThreadLocal));
+            try {
+                enqueue_factorization(F, F->capture_stream);
+            } catch (...) {
+                cudaStreamEndCapture(F->capture_stream, &g);
+                if (g) cudaGraphDestroy(g);
+                throw;
+            }
+            CK(cudaStreamEndCapture(F->capture_stream, &g));
+            F->factor_graph_nodes = (int)(g_launches.load() - before);
+            g_launches -= F->factor_graph_nodes;   // counted when the graph runs
+            cudaError_t e = cudaGraphInstantiate(&F->factor_graph, g, 0);
+            cudaGraphDestroy(g);
+            CK(e);
+        }
+        CK(cudaGraphLaunch(F->factor_graph, st));
+        counted(F->factor_graph_nodes);
     }
     PivotStats hs;
     CK(cudaMemcpyAsync(&hs, stats, sizeof(PivotStats), cudaMemcpyDeviceToHost, st));
@@ -514,6 +576,8 @@ uchol_factor_s* create_factor(uchol_symbolic_s* S, int n, int nnz, const uchol_o
         F->maps.upload(maps, st, "tensor maps");
         CK(cudaStreamSynchronize(st));
     }
+    if (cfg.tensor_core)
+        F->minv.alloc((size_t)std::max(1, P.diag_slots) * kMinvStride * sizeof(float), "diagonal-block inverses");
     F->diag.alloc((size_t)std::max(1, S->n) * sizeof(double), "pivots");
     F->linv.alloc((size_t)std::max<size_t>(1, P.inv_blocks.size()) * cfg.solve_block * cfg.solve_block * F->elem,
                   "inverse diagonal blocks");
@@ -521,6 +585,7 @@ uchol_factor_s* create_factor(uchol_symbolic_s* S, int n, int nnz, const uchol_o
     F->full_val.alloc((size_t)std::max<long long>(1, S->full_nnz) * sizeof(double), "matrix values");
     F->stats.alloc(sizeof(PivotStats), "statistics");
     F->ctl.alloc(sizeof(FactorCtl), "statistics");
+    prepare_factor_kernels(F.get());
     return F.release();
 }
 
@@ -909,7 +974,8 @@ int uchol_estimate_device_bytes(const uchol_symbolic_desc* d, const uchol_option
         const int64_t op = o.precision == UCHOL_PRECISION_BF16 ? 2 : 4;
         if (factor_bytes) *factor_bytes = P.factor_elems * elem;
         if (contribution_bytes) *contribution_bytes = P.contrib_elems * elem;
-        if (staging_bytes) *staging_bytes = cfg.tensor_core ? 2 * P.stage_elems * op : 0;
+        if (staging_bytes)
+            *staging_bytes = cfg.tensor_core ? 2 * P.stage_elems * op + (int64_t)P.diag_slots * kMinvStride * 4 : 0;
         if (levels) *levels = P.levels;
         if (launches) *launches = (int)P.launches.size();
     });

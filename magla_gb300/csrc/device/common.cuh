@@ -53,10 +53,10 @@ struct EaEntry {
     int a;             // child trailing column
 };
 
-struct PanelTask {     // FP64 pivot block [j0, j0+nb) of front s plus TRSM of rows [row0, row0+rows)
+struct PanelTask {     // pivot block [j0, j0+nb) of front s, or its solve for rows [row0, row0+rows)
     int s, j0, nb, row0, rows;
     int stage;         // 1: also write the K-major staging copies W = L D and L (tensor-core path)
-    int pad0;
+    int slot;          // mixed path: workspace slot of the block's inverse (index within its launch)
     int stage_zero_to; // > 0: also clear staging columns [j0 + nb, stage_zero_to) of these rows
 };
 

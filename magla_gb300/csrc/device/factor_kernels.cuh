@@ -1,6 +1,8 @@
-// Factorisation kernels shared by the FP64 and the mixed-precision paths.
-// Front storage type T is double (FP64 path) or float (mixed path); pivots,
-// D and the pivot-block arithmetic are always FP64.
+// Factorisation kernels: assembly, extend-add and small fronts for both
+// paths (front storage type T is double on the FP64 path, float on the mixed
+// path; their pivots are FP64), and the FP64 path's pivot block, TRSM and
+// right-looking updates.  The mixed path's panel kernels are in
+// panel_kernels.cuh.
 #pragma once
 
 #include <cfloat>
@@ -237,23 +239,13 @@ __global__ void __launch_bounds__(128) k_pivot_block(const PanelTask* __restrict
     if (tid == 0) acc.flush(st);
 }
 
-// Rows [row0, row0+rows) under the pivot block: Y = F21 L11^-T (forward
-// substitution per row), L21 = Y / D.  On the tensor-core path rows below
-// the outer block also write the K-major staging copies W = L21 D (A
-// operand) and L21 (B operand) of the trailing update.
-template <class T, class Op, class Cc, int NBMAX>
+// Rows [row0, row0+rows) under the pivot block (FP64 path): Y = F21 L11^-T
+// (forward substitution per row), L21 = Y / D.
+template <class T, class Cc, int NBMAX>
 __global__ void __launch_bounds__(128) k_trsm(const PanelTask* __restrict__ tasks, const SnDev* __restrict__ sn,
-                                              T* __restrict__ panel, const double* __restrict__ diag,
-                                              Op* __restrict__ stage_a, Op* __restrict__ stage_b,
-                                              const StageInfo* __restrict__ stage_info) {
+                                              T* __restrict__ panel, const double* __restrict__ diag) {
     __shared__ Cc L11[NBMAX * (NBMAX + 1)];
-    __shared__ double dpiv[NBMAX];
     __shared__ double dinv[NBMAX];
-    // staging rows of this task, transposed for coalesced stores (only the
-    // tensor-core path stages: its operand types are at most 4 bytes)
-    constexpr int kStageRows = sizeof(Op) <= 4 ? 128 : 1;
-    __shared__ Op sa[kStageRows * (NBMAX + 1)];
-    __shared__ Op sb[kStageRows * (NBMAX + 1)];
     const PanelTask tk = tasks[blockIdx.x];
     const SnDev d = sn[tk.s];
     const int nb = tk.nb, j0 = tk.j0, ld = NBMAX + 1;
@@ -263,10 +255,7 @@ __global__ void __launch_bounds__(128) k_trsm(const PanelTask* __restrict__ task
         int r = idx % nb, c = idx / nb;
         L11[r + c * ld] = r > c ? (Cc)P[(j0 + r) + (long long)(j0 + c) * d.ldp] : Cc(0);
     }
-    if (tid < nb) {
-        dpiv[tid] = diag[d.first_col + j0 + tid];
-        dinv[tid] = 1.0 / dpiv[tid];
-    }
+    if (tid < nb) dinv[tid] = 1.0 / diag[d.first_col + j0 + tid];
     __syncthreads();
     if (tid < tk.rows) {
         const int i = tk.row0 + tid;
@@ -281,32 +270,8 @@ __global__ void __launch_bounds__(128) k_trsm(const PanelTask* __restrict__ task
             }
         }
 #pragma unroll
-        for (int k = 0; k < NBMAX; ++k) {
-            if (k < nb) {
-                const double l = (double)y[k] * dinv[k];
-                P[i + (long long)(j0 + k) * d.ldp] = (T)l;
-                if (kStageRows > 1 && tk.stage) {
-                    sa[tid * ld + k] = (Op)(float)(l * dpiv[k]);
-                    sb[tid * ld + k] = (Op)(float)l;
-                }
-            }
-        }
-    }
-    if (kStageRows == 1 || !tk.stage) return;
-    __syncthreads();
-    // one warp per row: lanes store consecutive K columns of the row
-    const StageInfo g = stage_info[tk.s];
-    const int warp = tid >> 5, lane = tid & 31;
-    for (int r = warp; r < tk.rows; r += nt >> 5) {
-        const long long so = g.off + (long long)(tk.row0 + r) * g.ld;
-        for (int k = lane; k < nb; k += 32) {
-            stage_a[so + j0 + k] = sa[r * ld + k];
-            stage_b[so + j0 + k] = sb[r * ld + k];
-        }
-        for (int k = j0 + nb + lane; k < tk.stage_zero_to; k += 32) {
-            stage_a[so + k] = (Op)0.0f;
-            stage_b[so + k] = (Op)0.0f;
-        }
+        for (int k = 0; k < NBMAX; ++k)
+            if (k < nb) P[i + (long long)(j0 + k) * d.ldp] = (T)((double)y[k] * dinv[k]);
     }
 }
 

@@ -319,6 +319,29 @@ Plan build_plan(int n, int count, const int* first_column, const int* parent, co
                 }
                 if ((int)P.tc_jobs.size() > jb) P.launches.push_back({Launch::TcUpdate, jb, (int)P.tc_jobs.size() - jb, tiles});
             }
+            // mixed path: the whole outer block in two launches (diagonal block, then its rows below)
+            if (cfg.tensor_core) {
+                int qb = (int)P.pivot_tasks.size();
+                int pb = (int)P.panel_tasks.size();
+                int slot = 0;
+                for (int s : large) {
+                    const SnDev& d = P.sn[s];
+                    if (d.w <= k0) continue;
+                    int nbo = std::min(NB, d.w - k0);
+                    P.pivot_tasks.push_back({s, k0, nbo, k0 + nbo, 0, -1, slot, 0});
+                    int zero_to = (k0 + nbo == d.w && P.stage[s].ld > d.w) ? P.stage[s].ld : 0;
+                    for (int r = k0 + nbo; r < d.m; r += kSolveRowsPlan) {
+                        int rows = std::min(kSolveRowsPlan, d.m - r);
+                        P.panel_tasks.push_back({s, k0, nbo, r, rows, 1, slot, zero_to});
+                        P.panel_flops += 2.0 * rows * nbo * nbo;
+                    }
+                    ++slot;
+                }
+                P.diag_slots = std::max(P.diag_slots, slot);
+                if ((int)P.pivot_tasks.size() > qb) P.launches.push_back({Launch::DiagBlock, qb, (int)P.pivot_tasks.size() - qb, 0});
+                if ((int)P.panel_tasks.size() > pb) P.launches.push_back({Launch::PanelSolve, pb, (int)P.panel_tasks.size() - pb, 0});
+                continue;
+            }
             for (int j0r = 0; j0r < NB; j0r += PB) {
                 int qb = (int)P.pivot_tasks.size();
                 int pb = (int)P.panel_tasks.size();

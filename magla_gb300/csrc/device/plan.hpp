@@ -12,6 +12,8 @@
 
 namespace uchol_dev {
 
+constexpr int kSolveRowsPlan = 128;   // rows per panel-solve task (kSolveRows of the kernel)
+
 struct PlanConfig {
     int pivot_block = 32;     // FP64 pivot block (the reference's PanelWidth)
     int outer_block = 32;     // Schur-update block (== pivot_block on the FP64 path)
@@ -26,7 +28,8 @@ struct PlanConfig {
 // One kernel launch: a contiguous range of tasks in one of the task arrays.
 struct Launch {
     enum Kind : int {
-        ZeroContrib, ExtendAdd, SmallFronts, PivotBlock, Trsm, SimtUpdate, TcUpdate
+        ZeroContrib, ExtendAdd, SmallFronts, PivotBlock, Trsm, SimtUpdate, TcUpdate, DiagBlock, PanelSolve,
+        KindCount
     } kind;
     int begin, count;   // task range
     long long tiles;    // update launches: total tiles (= grid size)
@@ -72,8 +75,10 @@ struct Plan {
     std::vector<EaItem> ea_items;
     std::vector<EaEntry> ea_entries;
     std::vector<int> small_fronts;
-    std::vector<PanelTask> pivot_tasks;   // one per (front, pivot block)
-    std::vector<PanelTask> panel_tasks;   // TRSM row chunks
+    std::vector<PanelTask> pivot_tasks;   // one per (front, pivot block); mixed path: per (front, outer block)
+    std::vector<PanelTask> panel_tasks;   // TRSM / panel-solve row chunks
+    int diag_slots = 0;                   // mixed path: most diagonal blocks of one launch (inverse workspace slots)
+    double panel_flops = 0.0;             // mixed path: flops of the panel-solve products
     std::vector<UpdJob> simt_jobs;
     std::vector<TcJobHost> tc_jobs;
     std::vector<StageInfo> stage;              // per supernode (tensor-core path)

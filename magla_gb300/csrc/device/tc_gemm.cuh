@@ -402,10 +402,8 @@ inline void launch_tc_gemm(bool bf16, const TcJob* jobs, int njobs, long long ti
     const size_t smem = tc_smem_bytes();
     const unsigned grid = (unsigned)std::min<long long>(tiles, (long long)sms);
     if (bf16) {
-        cudaFuncSetAttribute(k_tc_gemm<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         k_tc_gemm<true><<<grid, kTcThreads, smem, st>>>(jobs, njobs, tiles, sn, panel, contrib, maps, status);
     } else {
-        cudaFuncSetAttribute(k_tc_gemm<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         k_tc_gemm<false><<<grid, kTcThreads, smem, st>>>(jobs, njobs, tiles, sn, panel, contrib, maps, status);
     }
 }
