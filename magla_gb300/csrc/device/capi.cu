@@ -185,6 +185,10 @@ struct uchol_factor_s {
     DBuf work, fv, fv2, vec[6], scal;   // solve workspace
     DBuf linv;                          // inverses of the diagonal blocks (solves)
     DBuf minv;                          // mixed path: per outer block X^T, D, D^{-1} of each diagonal block
+    DBuf solve_flags;                   // per diagonal block: forward and backward "solution published" flags
+    DBuf solve_maps;                    // per supernode: tensor map of the diagonal region of its panel
+    DBuf solve_status;                  // nonzero once a bounded wait of a solve expired
+    int coop_fwd = 0, coop_bwd = 0;     // resident CTAs of the level solve kernels (whole device)
     int ws_nrhs = 0;
     cudaStream_t capture_stream = nullptr;
     cudaGraphExec_t solve_graph = nullptr;
@@ -591,6 +595,35 @@ uchol_factor_s* create_factor(uchol_symbolic_s* S, int n, int nnz, const uchol_o
 
 // ---- solves ----
 
+// Cooperative launch: every CTA of the grid is resident at once (the level
+// solve kernels wait on one another), or the launch fails.
+template <class... KArgs, class... Args>
+void launch_cooperative(void (*kernel)(KArgs...), int grid, int block, size_t smem, cudaStream_t st, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    CK(cudaLaunchKernelEx(&cfg, kernel, args...));
+}
+
+// Reports an expired bounded wait of the level solve kernels (after a synchronisation).
+void check_solve_status(uchol_factor_s* F) {
+    if (!F->solve_status.p) return;
+    int h = 0;
+    CK(cudaMemcpy(&h, F->solve_status.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (h != 0) {
+        CK(cudaMemset(F->solve_status.p, 0, sizeof(int)));
+        throw Error(UCHOL_TIMEOUT, "a bounded device wait expired during a triangular solve (status " +
+                                       std::to_string(h) + ")");
+    }
+}
+
 template <class T, class Cv, int SB>
 void run_solve(uchol_factor_s* F, int nrhs, Cv* work, Cv* fv, Cv* fv2, cudaStream_t st) {
     uchol_symbolic_s* S = F->sym;
@@ -611,35 +644,64 @@ void run_solve(uchol_factor_s* F, int nrhs, Cv* work, Cv* fv, Cv* fv2, cudaStrea
     const Cv* linv = F->linv.as<Cv>();
     const SolveBlockTask* tasks = D.solve_tasks.as<SolveBlockTask>();
     const double* diag = F->diag.as<double>();
+    const int nblocks = (int)P.inv_blocks.size();
+    int* fwd_flags = F->solve_flags.as<int>();
+    int* bwd_flags = fwd_flags + nblocks;
+    int* progress = bwd_flags + nblocks;
+    int* status = F->solve_status.as<int>();
+    CK(cudaMemsetAsync(fwd_flags, 0, sizeof(int) * ((size_t)2 * nblocks + P.progress_count), st));
+    const size_t smem = SB * SB * (sizeof(T) + sizeof(Cv)) + kLevelSmemSlack;
+    auto level_args = [&](const SolveLaunch& L, int* flags, int grid) {
+        LevelArgs la;
+        la.chains = tasks + L.begin;
+        la.nchains = L.count;
+        la.bulk = tasks + L.bulk_begin;
+        la.nbulk = L.bulk_count;
+        // CTAs split between chains and bulk in proportion to their work (a block solve counted as
+        // two chunk updates), each side at least one
+        const double share = 2.0 * L.chain_work / std::max(1.0, 2.0 * L.chain_work + (double)L.bulk_work);
+        const int want = std::max(L.long_chains, (int)std::lround(grid * share));
+        la.nchain_cta = std::max(1, std::min({L.count, grid - 1, want}));
+        // bulk CTAs split between the diagonal-block chunks (which the chains wait for: weighted
+        // up) and the trailing-row chunks
+        const int nbulk_cta = grid - la.nchain_cta;
+        const long long trail_work = L.bulk_work - L.diag_work;
+        la.ndiag = L.ndiag;
+        if (L.ndiag == 0) {
+            la.ndiag_cta = 0;
+        } else if (L.ndiag == L.bulk_count) {
+            la.ndiag_cta = nbulk_cta;
+        } else {
+            const double dshare = 2.0 * L.diag_work / std::max(1.0, 2.0 * L.diag_work + (double)trail_work);
+            la.ndiag_cta = std::max(1, std::min(nbulk_cta - 1, (int)std::lround(nbulk_cta * dshare)));
+        }
+        la.steps = L.steps;
+        la.flags = flags;
+        la.progress = progress + L.progress_off;
+        la.status = status;
+        la.maps = F->solve_maps.as<CUtensorMap>();
+        return la;
+    };
     for (const SolveLaunch& L : P.fwd_launches) {
         if (L.count == 0) continue;
-        switch (L.kind) {
-            case SolveLaunch::FwdGather: k_fwd_gather<Cv><<<L.count, 256, 0, st>>>(tasks + L.begin, A, work, fv); break;
-            case SolveLaunch::FwdStart:
-                k_block_start<Cv, SB, true><<<L.count, 256, SB * SB * sizeof(Cv), st>>>(tasks + L.begin, A, linv, fv, fv2);
-                break;
-            case SolveLaunch::FwdBlock:
-                k_fwd_block<T, Cv, SB><<<L.count, 128, SB * SB * sizeof(Cv), st>>>(tasks + L.begin, A, panel, linv, fv,
-                                                                                   fv2);
-                break;
-            case SolveLaunch::FwdFinish: k_fwd_finish<Cv><<<L.count, 256, 0, st>>>(tasks + L.begin, A, diag, fv2, work); break;
-            default: break;
+        if (L.kind == SolveLaunch::FwdGather) {
+            k_fwd_gather<Cv><<<L.count, 256, 0, st>>>(tasks + L.begin, A, work, fv);
+        } else {
+            const int grid = F->coop_fwd;
+            launch_cooperative(k_fwd_level<T, Cv, SB>, grid, 256, smem, st, level_args(L, fwd_flags, grid), A, panel,
+                               linv, fv, fv2, diag, work);
         }
     }
     for (const SolveLaunch& L : P.bwd_launches) {
         if (L.count == 0) continue;
-        switch (L.kind) {
-            case SolveLaunch::BwdGather: k_bwd_gather<Cv><<<L.count, 256, 0, st>>>(tasks + L.begin, A, work, fv); break;
-            case SolveLaunch::BwdTail: k_bwd_cols<T, Cv><<<L.count, 256, 0, st>>>(tasks + L.begin, A, panel, fv); break;
-            case SolveLaunch::BwdStart:
-                k_block_start<Cv, SB, false><<<L.count, 256, SB * SB * sizeof(Cv), st>>>(tasks + L.begin, A, linv, fv, fv2);
-                break;
-            case SolveLaunch::BwdBlock:
-                k_bwd_block<T, Cv, SB><<<L.count, 256, SB * SB * sizeof(Cv), st>>>(tasks + L.begin, A, panel, linv, fv,
-                                                                                   fv2);
-                break;
-            case SolveLaunch::BwdFinish: k_bwd_finish<Cv><<<L.count, 256, 0, st>>>(tasks + L.begin, A, fv2, work); break;
-            default: break;
+        if (L.kind == SolveLaunch::BwdGather) {
+            k_bwd_gather<Cv><<<L.count, 256, 0, st>>>(tasks + L.begin, A, work, fv);
+        } else if (L.kind == SolveLaunch::BwdTail) {
+            k_bwd_cols<T, Cv><<<L.count, 256, 0, st>>>(tasks + L.begin, A, panel, fv);
+        } else {
+            const int grid = F->coop_bwd;
+            launch_cooperative(k_bwd_level<T, Cv, SB>, grid, 256, smem, st, level_args(L, bwd_flags, grid), A, panel,
+                               linv, fv, fv2, work);
         }
     }
     CK(cudaGetLastError());
@@ -649,7 +711,7 @@ int solve_launch_count(const Plan& P) {
     int c = 0;
     for (const SolveLaunch& L : P.fwd_launches) c += L.count > 0;
     for (const SolveLaunch& L : P.bwd_launches) c += L.count > 0;
-    return c;
+    return c + 1;   // + the flag reset
 }
 
 // The triangular solves of a factor for nrhs columns, captured once into a
@@ -662,14 +724,45 @@ void launch_solve_graph(uchol_factor_s* F, int nrhs, Cv* work, cudaStream_t st) 
             F->solve_graph = nullptr;
         }
         if (!F->capture_stream) CK(cudaStreamCreateWithFlags(&F->capture_stream, cudaStreamNonBlocking));
-        CK(cudaFuncSetAttribute(k_fwd_block<T, Cv, SB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)(SB * SB * sizeof(Cv))));
-        CK(cudaFuncSetAttribute(k_bwd_block<T, Cv, SB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)(SB * SB * sizeof(Cv))));
-        CK(cudaFuncSetAttribute(k_block_start<Cv, SB, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)(SB * SB * sizeof(Cv))));
-        CK(cudaFuncSetAttribute(k_block_start<Cv, SB, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)(SB * SB * sizeof(Cv))));
+        // the level kernels run as cooperative launches: at most as many CTAs as the device holds at once
+        const int smem = (int)(SB * SB * (sizeof(T) + sizeof(Cv)) + kLevelSmemSlack);
+        CK(cudaFuncSetAttribute(k_fwd_level<T, Cv, SB>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        CK(cudaFuncSetAttribute(k_bwd_level<T, Cv, SB>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        int per_sm = 0;
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fwd_level<T, Cv, SB>, 256, smem));
+        F->coop_fwd = per_sm * F->sms;
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bwd_level<T, Cv, SB>, 256, smem));
+        F->coop_bwd = per_sm * F->sms;
+        if (F->coop_fwd < 2 || F->coop_bwd < 2) throw Error(UCHOL_CUDA_ERROR, "the level solve kernels do not fit");
+        if (!F->solve_maps.p) {
+            // tile copies of the level solves: each front's panel (m x w)
+            const Plan& P = F->dp->plan;
+            std::vector<CUtensorMap> maps(std::max(1, (int)P.sn.size()));
+            std::memset(maps.data(), 0, maps.size() * sizeof(CUtensorMap));
+            const size_t es = sizeof(T);
+            for (size_t s2 = 0; s2 < P.sn.size(); ++s2) {
+                const SnDev& d = P.sn[s2];   // every front: its trailing rows are bulk tiles too
+                cuuint64_t dims[2] = {(cuuint64_t)d.m, (cuuint64_t)d.w};
+                cuuint64_t strides[1] = {(cuuint64_t)d.ldp * es};
+                cuuint32_t box[2] = {(cuuint32_t)SB, (cuuint32_t)SB};
+                cuuint32_t estr[2] = {1, 1};
+                CUresult r = tensor_map_encoder()(&maps[s2], es == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
+                                                  2, (char*)F->panel.p + (size_t)d.panel_off * es, dims, strides, box,
+                                                  estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                if (r != CUDA_SUCCESS)
+                    throw Error(UCHOL_CUDA_ERROR, "cuTensorMapEncodeTiled failed for a solve tile map: " + std::to_string((int)r));
+            }
+            F->solve_maps.upload(maps, st, "solve tile maps");
+            CK(cudaStreamSynchronize(st));
+        }
+        if (!F->solve_flags.p) {
+            const Plan& P = F->dp->plan;
+            F->solve_flags.alloc(sizeof(int) * (2 * std::max<size_t>(1, P.inv_blocks.size()) + P.progress_count),
+                                 "solve flags");
+            F->solve_status.alloc(sizeof(int), "solve flags");
+            CK(cudaMemsetAsync(F->solve_status.p, 0, sizeof(int), st));
+        }
         cudaGraph_t g = nullptr;
         CK(cudaStreamBeginCapture(F->capture_stream, cudaStreamCaptureModeThreadLocal));
         try {
@@ -839,6 +932,7 @@ void solve_refined(uchol_factor_s* F, int nrhs, const double* b, int ldb, double
     }
     CK(cudaGetLastError());
     double ms = timer.stop();
+    check_solve_status(F);
     if (rs) *rs = {it, current, initial, ms};
     if (current > opt.tolerance)
         throw Error(UCHOL_NO_CONVERGENCE, "refinement stopped at relative residual " + std::to_string(current) +
@@ -1090,6 +1184,7 @@ int uchol_solve_device(uchol_factor f, int n, int nrhs, const double* b, int ldb
         ensure_workspace(f, nrhs);
         apply_factor(f, nrhs, b, ldb, x, ldx);
         CK(cudaStreamSynchronize(f->sym->stream));
+        check_solve_status(f);
     });
 }
 
@@ -1106,6 +1201,7 @@ int uchol_solve(uchol_factor f, int n, int nrhs, const double* b, int ldb, doubl
         apply_factor(f, nrhs, db, n, dx, n);
         CK(cudaMemcpy2DAsync(x, (size_t)ldx * 8, dx, (size_t)n * 8, (size_t)n * 8, nrhs, cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
+        check_solve_status(f);
     });
 }
 

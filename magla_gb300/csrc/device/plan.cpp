@@ -430,93 +430,86 @@ Plan build_plan(int n, int count, const int* first_column, const int* parent, co
         for (int k0 = 0; k0 < P.sn[s].w; k0 += SB)
             P.inv_blocks.push_back({s, k0, std::min(SB, P.sn[s].w - k0), 0, 0, 1, (int)P.inv_blocks.size()});
     }
-    const int kRowChunk = SB, kColChunk = SB;
     constexpr int kGatherChunk = 2048;
-    // chunked per-front tasks: rows [r0, r1) of the front vector (gathers) or
-    // own columns [r0, r1) (finishes)
-    auto chunk_tasks = [&](const std::vector<int>& fronts, bool own_columns) {
+    // chunked per-front tasks: rows [r0, r1) of the front vector
+    auto gather_tasks = [&](const std::vector<int>& fronts) {
         int b = (int)P.solve_tasks.size();
-        for (int s : fronts) {
-            const int lim = own_columns ? P.sn[s].w : P.sn[s].m;
-            for (int r = 0; r < lim; r += kGatherChunk)
-                P.solve_tasks.push_back({s, 0, 0, r, std::min(lim, r + kGatherChunk), 0, 0});
-        }
+        for (int s : fronts)
+            for (int r = 0; r < P.sn[s].m; r += kGatherChunk)
+                P.solve_tasks.push_back({s, 0, 0, r, std::min(P.sn[s].m, r + kGatherChunk), 0, 0});
         return std::make_pair(b, (int)P.solve_tasks.size() - b);
+    };
+    // level launch: chains (one per front), then the bulk chunks that take updates.  The
+    // diagonal-block chunks of a front that the bulk updates are contiguous and in block order,
+    // from block 2 (forward; blocks 0 and 1 take theirs from the chain) or block 0 up to
+    // nblk - 3 (backward); the chain finds them by index (task k0 = the index its block-0
+    // chunk would have).  Trailing-row chunks (forward only) come after all of them.
+    auto level_launch = [&](SolveLaunch::Kind kind, const std::vector<int>& fronts, bool forward) {
+        SolveLaunch Lh{kind, (int)P.solve_tasks.size(), (int)fronts.size(), 0, 0, 0, P.progress_count, 0, 0, 0, 0, 0};
+        std::vector<SolveBlockTask> bulk;
+        // chains longest first: CTA k takes chains k, k + nchain_cta, ..., so every long chain
+        // gets a CTA of its own when there are enough
+        std::vector<int> order(fronts.begin(), fronts.end());
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return P.sn[a].w > P.sn[b].w; });
+        for (int s : order) Lh.long_chains += (P.sn[s].w + SB - 1) / SB >= 3;
+        const size_t chain_base = P.solve_tasks.size();
+        P.solve_tasks.resize(chain_base + order.size());
+        std::map<int, int> pos;
+        for (size_t k = 0; k < order.size(); ++k) pos[order[k]] = (int)k;
+        for (int s : fronts) {
+            const SnDev& d = P.sn[s];
+            const int nblk = (d.w + SB - 1) / SB;
+            Lh.steps = std::max(Lh.steps, nblk);
+            Lh.chain_work += nblk;
+            Lh.bulk_work += (long long)std::max(0, nblk - 1) * (nblk - 2 > 0 ? nblk - 2 : 0) / 2;
+            const int lo = forward ? 2 : 0, hi = forward ? nblk - 1 : nblk - 3;   // bulk diagonal blocks [lo, hi]
+            P.solve_tasks[chain_base + pos[s]] = {s, (int)bulk.size() - lo, nblk, 0, 0, 0, first_blk[s]};
+            // kn: the number of solutions the chunk applies (forward y_0 .. y_{k-2}; backward
+            // x_{nblk-1} .. x_{k+2}); backward k0 = nblk - 1 (step t applies block k0 - t)
+            for (int k = lo; k <= hi; ++k)
+                bulk.push_back({s, forward ? 0 : nblk - 1, forward ? k - 1 : nblk - 2 - k, k * SB,
+                                std::min(d.w, (k + 1) * SB), 0, first_blk[s]});
+        }
+        Lh.ndiag = (int)bulk.size();
+        Lh.diag_work = Lh.bulk_work;
+        const bool trailing = forward;
+        if (trailing)
+            for (int s : fronts) {
+                const SnDev& d = P.sn[s];
+                const int nblk = (d.w + SB - 1) / SB;
+                // SB - A rows each: the tile copy starts at the row rounded down to 16 bytes
+                // (A rows), so that the chunk still fits in one SB-row box
+                const int height = SB - kTileAlignRows(cfg);
+                for (int r = d.w; r < d.m; r += height) {
+                    bulk.push_back({s, 0, nblk, r, std::min(d.m, r + height), 0, first_blk[s]});
+                    Lh.bulk_work += nblk;
+                }
+            }
+        Lh.bulk_begin = (int)P.solve_tasks.size();
+        Lh.bulk_count = (int)bulk.size();
+        P.solve_tasks.insert(P.solve_tasks.end(), bulk.begin(), bulk.end());
+        P.progress_count += (int)bulk.size();
+        return Lh;
     };
     for (int L = 0; L < P.levels; ++L) {
         const auto& fronts = at_level[L];
-        {
-            auto g = chunk_tasks(fronts, false);
-            P.fwd_launches.push_back({SolveLaunch::FwdGather, g.first, g.second});
-            int sb = (int)P.solve_tasks.size();
-            for (int s : fronts)
-                P.solve_tasks.push_back({s, 0, std::min(SB, P.sn[s].w), 0, 0, 0, first_blk[s]});
-            P.fwd_launches.push_back({SolveLaunch::FwdStart, sb, (int)P.solve_tasks.size() - sb});
-        }
-        int max_w = 0;
-        for (int s : fronts) max_w = std::max(max_w, P.sn[s].w);
-        for (int k0 = 0; k0 < max_w; k0 += SB) {
-            int tb = (int)P.solve_tasks.size();
-            for (int s : fronts) {
-                const SnDev& d = P.sn[s];
-                if (d.w <= k0) continue;
-                int kn = std::min(SB, d.w - k0);
-                int blk = first_blk[s] + k0 / SB;
-                for (int r = k0 + kn; r < d.m; r += kRowChunk) {
-                    const int fl = (r == k0 + kn && r < d.w) ? kSolveNext : 0;   // rows [r, r+SB) are the next block
-                    P.solve_tasks.push_back({s, k0, kn, r, std::min(d.m, r + kRowChunk), fl, blk});
-                }
-            }
-            P.fwd_launches.push_back({SolveLaunch::FwdBlock, tb, (int)P.solve_tasks.size() - tb});
-        }
-        {
-            auto g = chunk_tasks(fronts, true);
-            P.fwd_launches.push_back({SolveLaunch::FwdFinish, g.first, g.second});
-        }
+        auto g = gather_tasks(fronts);
+        P.fwd_launches.push_back({SolveLaunch::FwdGather, g.first, g.second, 0, 0, 0, 0, 0, 0, 0, 0, 0});
+        P.fwd_launches.push_back(level_launch(SolveLaunch::FwdLevel, fronts, true));
     }
     for (int L = P.levels - 1; L >= 0; --L) {
         const auto& fronts = at_level[L];
-        {
-            auto g = chunk_tasks(fronts, false);
-            P.bwd_launches.push_back({SolveLaunch::BwdGather, g.first, g.second});
-        }
+        auto g = gather_tasks(fronts);
+        P.bwd_launches.push_back({SolveLaunch::BwdGather, g.first, g.second, 0, 0, 0, 0, 0, 0, 0, 0, 0});
         int tb = (int)P.solve_tasks.size();
         for (int s : fronts) {
             const SnDev& d = P.sn[s];
             if (d.m == d.w) continue;
             for (int c = 0; c < d.w; c += 8) P.solve_tasks.push_back({s, c, std::min(8, d.w - c), d.w, d.m, 0, 0});
         }
-        if ((int)P.solve_tasks.size() > tb) P.bwd_launches.push_back({SolveLaunch::BwdTail, tb, (int)P.solve_tasks.size() - tb});
-        {
-            int sb = (int)P.solve_tasks.size();
-            for (int s : fronts) {
-                const int nbk = (P.sn[s].w + SB - 1) / SB;
-                const int k0 = (nbk - 1) * SB;
-                P.solve_tasks.push_back({s, k0, P.sn[s].w - k0, 0, 0, 0, first_blk[s] + nbk - 1});
-            }
-            P.bwd_launches.push_back({SolveLaunch::BwdStart, sb, (int)P.solve_tasks.size() - sb});
-        }
-        int max_w = 0;
-        for (int s : fronts) max_w = std::max(max_w, P.sn[s].w);
-        int blocks = (max_w + SB - 1) / SB;
-        for (int b = blocks - 1; b >= 0; --b) {
-            int k0 = b * SB;
-            int tb2 = (int)P.solve_tasks.size();
-            for (int s : fronts) {
-                const SnDev& d = P.sn[s];
-                if (d.w <= k0) continue;
-                int kn = std::min(SB, d.w - k0);
-                int blk = first_blk[s] + b;
-                // column chunks aligned to the blocks: the chunk [k0 - SB, k0) is the previous block
-                for (int c = k0 - SB; c >= 0; c -= kColChunk)
-                    P.solve_tasks.push_back({s, k0, kn, c, c + kColChunk, c == k0 - SB ? kSolveNext : 0, blk});
-            }
-            P.bwd_launches.push_back({SolveLaunch::BwdBlock, tb2, (int)P.solve_tasks.size() - tb2});
-        }
-        {
-            auto g = chunk_tasks(fronts, true);
-            P.bwd_launches.push_back({SolveLaunch::BwdFinish, g.first, g.second});
-        }
+        if ((int)P.solve_tasks.size() > tb)
+            P.bwd_launches.push_back({SolveLaunch::BwdTail, tb, (int)P.solve_tasks.size() - tb, 0, 0, 0, 0, 0, 0, 0, 0, 0});
+        P.bwd_launches.push_back(level_launch(SolveLaunch::BwdLevel, fronts, false));
     }
     return P;
 }

@@ -36,17 +36,23 @@ struct Launch {
 };
 
 struct SolveLaunch {
-    enum Kind : int {
-        FwdGather, FwdStart, FwdBlock, FwdFinish, BwdGather, BwdTail, BwdStart, BwdBlock, BwdFinish
-    } kind;
-    int begin, count;
+    enum Kind : int { FwdGather, FwdLevel, BwdGather, BwdTail, BwdLevel } kind;
+    int begin, count;   // tasks; level launches: the chains (one per front)
+    int steps;          // level launches: most diagonal blocks of one front of the level
+    int bulk_begin, bulk_count;   // level launches: the bulk chunks
+    int progress_off;             // level launches: first progress counter of the bulk chunks
+    long long chain_work, bulk_work;   // level launches: block solves and chunk updates (CTA split)
+    int long_chains;                   // level launches: fronts of three or more diagonal blocks
+    int ndiag;                         // level launches: bulk chunks [0, ndiag) are diagonal blocks
+    long long diag_work;               // level launches: chunk updates of those
 };
 
-// Diagonal block [k0, k0+kn) of supernode s (its inverse is block `blk` of the
-// inverse arena); rows (forward) or columns (backward) [r0, r1) updated with
-// the block's solution.  Flag kSolveNext: this task's rows (columns) are the
-// next block; after the update it computes and stores that block's solution.
-constexpr int kSolveNext = 4;
+// Solve task of supernode s.  Gathers: rows [r0, r1) of the front vector.
+// Level launches: a chain (k0 = bulk index of the chunk of the front's
+// diagonal block 0, blk = its first diagonal block) or a bulk chunk of rows
+// (forward) or own columns (backward) [r0, r1) (blk as for chains).
+// Trailing-row dots: columns [k0, k0+kn) against rows [r0, r1).  Inversion:
+// diagonal block [k0, k0+kn), blk = its index in the inverse arena.
 struct SolveBlockTask {
     int s, k0, kn, r0, r1;
     int flags, blk;
@@ -57,6 +63,10 @@ struct TcJobHost {
     long long tile_begin;
     int s, c0, cend, kbeg, kn, map;
 };
+
+// Rows in 16 bytes of the factor storage type (float on the tensor-core path, else double):
+// tile copies by tensor map must start on a multiple of it.
+inline int kTileAlignRows(const PlanConfig& cfg) { return cfg.tensor_core ? 4 : 2; }
 
 struct Plan {
     PlanConfig cfg;
@@ -94,6 +104,7 @@ struct Plan {
     std::vector<SolveBlockTask> solve_tasks;
     std::vector<SolveBlockTask> inv_blocks;    // every diagonal block, for the inversion after a factorisation
     std::vector<SolveLaunch> fwd_launches, bwd_launches;
+    int progress_count = 0;                    // progress counters of all level launches
 };
 
 // Throws std::runtime_error on inconsistent symbolic input.

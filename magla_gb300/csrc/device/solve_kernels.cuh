@@ -11,6 +11,8 @@
 // only the order of the floating-point sums differs.
 #pragma once
 
+#include <cuda.h>
+
 #include "common.cuh"
 #include "plan.hpp"
 
@@ -126,192 +128,615 @@ __global__ void __launch_bounds__(SB) k_invert_blocks(const SolveBlockTask* __re
     }
 }
 
-__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((unsigned)__cvta_generic_to_shared(smem)),
-                 "l"(gmem)
+// ---- persistent block solves: one cooperative launch per tree level ----
+//
+// The diagonal blocks of a front must be solved in order, and each block
+// solution updates every row (forward) or column (backward) after it.  One
+// kernel per level runs the whole chain with two kinds of CTA, all resident
+// at once (cooperative launch):
+//   chain CTAs (one or more fronts each) solve the blocks in order.  For
+//     block b+1 a chain needs the rows (columns) of that block updated with
+//     every earlier solution: all but the latest come from the bulk CTAs (it
+//     waits for the chunk's progress counter), the latest it applies itself
+//     from an SB x SB tile of L that it prefetched into shared memory, with
+//     the block's inverse, while it waited.  It then publishes the block's
+//     solution with a release flag.
+//   bulk CTAs own chunks of SB rows (columns) and apply each published
+//     solution to them, then advance the chunk's progress counter.
+// Everything proceeds step-major: a wait at step b is only ever for a flag
+// or counter of step b-1, so no CTA can block its own producer.
+
+constexpr unsigned long long kSolveWaitNs = 1000000000ull;   // 1 s per bounded wait
+constexpr size_t kLevelSmemSlack = 1024;                      // alignment slack of the level kernels' dynamic smem
+constexpr int kSolveStatusTimeout = 2;
+
+__device__ __forceinline__ unsigned long long solve_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+__device__ __forceinline__ int ld_acquire_gpu(const int* p) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_gpu(int* p, int v) {
+    asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Bulk copies global -> shared on an mbarrier (the copy engine moves the
+// bytes; the issuing threads do not wait for them).
+__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void bar_init(unsigned long long* bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void bar_expect(unsigned long long* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
                  : "memory");
 }
-__device__ __forceinline__ void cp_async_wait_all() {
-    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;" ::: "memory");
-}
-
-// Starts copying inverse block `src` (SB x SB) into shared memory.
-template <class Cv, int SB>
-__device__ __forceinline__ void prefetch_inverse(Cv* dst, const Cv* src) {
-    constexpr int chunks = SB * SB * (int)sizeof(Cv) / 16;
-    for (int q = threadIdx.x; q < chunks; q += blockDim.x) cp_async16(reinterpret_cast<char*>(dst) + 16 * q,
-                                                                       reinterpret_cast<const char*>(src) + 16 * q);
-}
-
-// First block solution of each front: forward y_0 = L_00^-1 f_0 (after the
-// gather), backward x_last = L_ll^-T g_last (after the trailing-row dots).
-template <class Cv, int SB, bool FORWARD>
-__global__ void __launch_bounds__(256) k_block_start(const SolveBlockTask* __restrict__ tasks, SolveArgs A,
-                                                     const Cv* __restrict__ linv, const Cv* __restrict__ fv,
-                                                     Cv* __restrict__ sol) {
-    extern __shared__ __align__(16) unsigned char blk_smem[];
-    Cv* Ls = reinterpret_cast<Cv*>(blk_smem);
-    __shared__ Cv v[SB];
-    const SolveBlockTask tk = tasks[blockIdx.x];
-    const int kn = tk.kn;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
-    prefetch_inverse<Cv, SB>(Ls, linv + (long long)tk.blk * SB * SB);
-    cp_async_wait_all();
-    for (int r = 0; r < A.nrhs; ++r) {
-        const long long base = A.fvec_off[tk.s] + r * A.fv_stride;
-        __syncthreads();
-        for (int t = threadIdx.x; t < kn; t += blockDim.x) v[t] = fv[base + tk.k0 + t];
-        __syncthreads();
-        if (FORWARD) {
-            // thread per output row: consecutive threads read consecutive words of each inverse column
-            for (int t = threadIdx.x; t < kn; t += blockDim.x) {
-                Cv acc = Cv(0);
-                for (int k = 0; k <= t; ++k) acc += Ls[t + k * SB] * v[k];
-                sol[base + tk.k0 + t] = acc;
-            }
-        } else {
-            // warp per output: lanes read consecutive words of one inverse column
-            for (int t = warp; t < kn; t += nwarps) {
-                Cv acc = Cv(0);
-                for (int k = t + lane; k < kn; k += 32) acc += Ls[k + t * SB] * v[k];
-                for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-                if (lane == 0) sol[base + tk.k0 + t] = acc;
-            }
+// Waits (bounded) for phase `parity` of the mbarrier; false if the wait expired.
+__device__ __forceinline__ bool bar_wait(unsigned long long* bar, unsigned parity, int* status) {
+    const unsigned long long t0 = solve_ns();
+    for (;;) {
+        unsigned done;
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
+            : "=r"(done)
+            : "r"(smem_addr(bar)), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if (solve_ns() - t0 > kSolveWaitNs) {
+            atomicExch(status, kSolveStatusTimeout);
+            return false;
         }
     }
 }
 
-// Forward step of diagonal block b of a front: y_b (in the solution buffer)
-// updates the task's rows, f[i] -= L[i, b] y_b.  The task whose rows are
-// block b+1 then computes y_{b+1} from their final values with the inverse
-// it prefetched at the start.
+// Thread 0 starts the copy of the SB x SB tile of L at rows [r0, r0+SB),
+// columns [c0, c0+SB) of a front's diagonal region (one tensor-map copy: a
+// column-major box, rows past the region read as zero) and of the first
+// inv_cols columns of an inverse block (SB x SB, contiguous) into shared
+// memory, completing on `bar`.
 template <class T, class Cv, int SB>
-__global__ void __launch_bounds__(128) k_fwd_block(const SolveBlockTask* __restrict__ tasks, SolveArgs A,
-                                                   const T* __restrict__ panel, const Cv* __restrict__ linv,
-                                                   Cv* __restrict__ fv, Cv* __restrict__ yv) {
-    extern __shared__ __align__(16) unsigned char blk_smem[];
-    Cv* Ls = reinterpret_cast<Cv*>(blk_smem);
-    __shared__ Cv y[SB];
-    __shared__ Cv fn[SB];
-    const SolveBlockTask tk = blocks_or_tasks(tasks);
-    const SnDev d = A.sn[tk.s];
-    const T* P = panel + d.panel_off;
-    const int kn = tk.kn;
-    const bool next = tk.flags & kSolveNext;
-    const int kn_next = next ? min(SB, d.w - (tk.k0 + kn)) : 0;
-    if (next) prefetch_inverse<Cv, SB>(Ls, linv + (long long)(tk.blk + 1) * SB * SB);
-    for (int r = 0; r < A.nrhs; ++r) {
-        const long long base = A.fvec_off[tk.s] + r * A.fv_stride;
-        Cv* f = fv + base;
-        __syncthreads();
-        for (int t = threadIdx.x; t < kn; t += blockDim.x) y[t] = yv[base + tk.k0 + t];
-        __syncthreads();
-        const int i = tk.r0 + threadIdx.x;
-        if (i < tk.r1) {
-            const T* row = P + i + (long long)tk.k0 * d.ldp;
-            Cv acc[4] = {Cv(0), Cv(0), Cv(0), Cv(0)};
-            int k = 0;
-            for (; k + 32 <= kn; k += 32) {
-                T vv[32];
-#pragma unroll
-                for (int u = 0; u < 32; ++u) vv[u] = row[(long long)(k + u) * d.ldp];
-#pragma unroll
-                for (int u = 0; u < 32; ++u) acc[u & 3] += (Cv)vv[u] * y[k + u];
-            }
-            for (; k < kn; ++k) acc[0] += (Cv)row[(long long)k * d.ldp] * y[k];
-            const Cv nv = f[i] - ((acc[0] + acc[1]) + (acc[2] + acc[3]));
-            f[i] = nv;
-            if (next && threadIdx.x < kn_next) fn[threadIdx.x] = nv;
-        }
-        if (next) {
-            if (r == 0) cp_async_wait_all();
-            __syncthreads();
-            for (int t = threadIdx.x; t < kn_next; t += blockDim.x) {
-                Cv acc = Cv(0);
-                for (int k = 0; k <= t; ++k) acc += Ls[t + k * SB] * fn[k];
-                yv[base + tk.k0 + kn + t] = acc;
+__device__ __forceinline__ void start_tile_copy(T* Tl, Cv* Li, const CUtensorMap* map, int r0, int c0,
+                                                bool with_tile, const Cv* inv, int inv_cols, unsigned long long* bar) {
+    if (threadIdx.x != 0) return;
+    const unsigned inv_bytes = (unsigned)(inv_cols * SB * sizeof(Cv));
+    const unsigned total = (with_tile ? (unsigned)(SB * SB * sizeof(T)) : 0u) + inv_bytes;
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    bar_expect(bar, total);
+    if (with_tile)
+        asm volatile(
+            "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+                smem_addr(Tl)),
+            "l"(reinterpret_cast<unsigned long long>(map)), "r"(r0), "r"(c0), "r"(smem_addr(bar))
+            : "memory");
+    bulk_g2s(Li, inv, inv_bytes, bar);
+}
+
+// Thread 0 waits for *flag >= target, giving up after kSolveWaitNs (status :=
+// timeout) or as soon as another CTA has given up; the CTA learns the outcome.
+__device__ __forceinline__ bool wait_at_least(const int* flag, int target, int* status, int* ok) {
+    if (threadIdx.x == 0) {
+        int good = 1;
+        if (ld_acquire_gpu(flag) < target) {
+            const unsigned long long t0 = solve_ns();
+            unsigned ns = 32;
+            for (;;) {
+                __nanosleep(ns);
+                if (ld_acquire_gpu(flag) >= target) break;
+                if (ns < 256) ns <<= 1;
+                if (ld_acquire_gpu(status) != 0) {
+                    good = 0;
+                    break;
+                }
+                if (solve_ns() - t0 > kSolveWaitNs) {
+                    atomicExch(status, kSolveStatusTimeout);
+                    good = 0;
+                    break;
+                }
             }
         }
+        *ok = good;
+    }
+    __syncthreads();
+    const bool r = *ok != 0;
+    __syncthreads();
+    return r;
+}
+
+// Every thread's writes, then the flag (release).
+__device__ __forceinline__ void publish(int* flag, int value) {
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) st_release_gpu(flag, value);
+}
+
+// A level launch.  chains: the level's fronts (task: s; blk = first diagonal
+// block; k0 = bulk index of the chunk of its block 0, its other diagonal
+// blocks following in order), taken round-robin by CTAs [0, nchain_cta).
+// bulk: the chunks, taken round-robin by the other CTAs.
+struct LevelArgs {
+    const SolveBlockTask* chains;
+    int nchains;
+    const SolveBlockTask* bulk;
+    int nbulk;
+    int nchain_cta;
+    int steps;       // most diagonal blocks of one front
+    int* flags;      // per diagonal block: solution published
+    int* progress;   // per bulk chunk: solutions applied
+    int* status;
+    const CUtensorMap* maps;   // per supernode: its panel (m x w)
+    int ndiag;                 // bulk chunks [0, ndiag): diagonal blocks, taken by bulk CTAs [0, ndiag_cta)
+    int ndiag_cta;             // the other bulk CTAs take the trailing-row chunks
+};
+
+// Tile copy of a bulk item into a stage buffer: rows [x, x+SB), columns
+// [y, y+SB) of a front's panel (zero past its m rows and w columns).
+template <class T, int SB>
+__device__ __forceinline__ void start_bulk_tile(T* dst, const CUtensorMap* map, int x, int y, unsigned long long* bar) {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    bar_expect(bar, (unsigned)(SB * SB * sizeof(T)));
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+            smem_addr(dst)),
+        "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(smem_addr(bar))
+        : "memory");
+}
+
+// The bulk CTA's share of the chunks: diagonal-block chunks or trailing-row chunks.
+struct BulkRange {
+    int begin, end, step;
+};
+__device__ __forceinline__ BulkRange bulk_range(const LevelArgs& L) {
+    const int k = blockIdx.x - L.nchain_cta, nbulk_cta = gridDim.x - L.nchain_cta;
+    if (k < L.ndiag_cta) return {k, L.ndiag, L.ndiag_cta};
+    return {L.ndiag + (k - L.ndiag_cta), L.nbulk, nbulk_cta - L.ndiag_cta};
+}
+
+// Next duty (front index q, step b) of a chain CTA after (q, b), in step-major
+// order; false when there is none.  Front q (chain task kn = its number of
+// diagonal blocks) has duties at steps -1 .. nblk - 2 (step b solves block
+// b + 1).
+__device__ __forceinline__ bool next_chain_duty(const LevelArgs& L, int& q, int& b, int nblk_q) {
+    if (q >= 0 && (int)blockIdx.x + L.nchain_cta >= L.nchains) {
+        // the CTA's only front (nblk_q: its number of diagonal blocks)
+        if (b + 1 < nblk_q - 1) {
+            ++b;
+            return true;
+        }
+        return false;
+    }
+    int nq = q < 0 ? (int)blockIdx.x : q + L.nchain_cta, nb = q < 0 ? -1 : b;
+    for (;;) {
+        if (nq >= L.nchains) {
+            nq = blockIdx.x;
+            if (++nb >= L.steps - 1) return false;
+        }
+        if (nb < L.chains[nq].kn - 1) {
+            q = nq;
+            b = nb;
+            return true;
+        }
+        nq += L.nchain_cta;
     }
 }
 
-// Backward step of diagonal block b of a front: x_b (in the solution buffer)
-// updates the task's columns c < k0, g[c] -= L[b, c]^T x_b (warp-cooperative
-// dots, four columns per warp pass).  The task whose columns are block b-1
-// then computes x_{b-1}.
+// Forward.  Chain duty (front, b): y_{b+1} = L_{b+1}^-1 (f_{b+1} - L[b+1, b] y_b),
+// where the bulk has already applied y_0 .. y_{b-1} to f_{b+1}; writes y and
+// y / D (the work vector).  Bulk chunk of diagonal block `own` applies
+// y_0 .. y_{own-2}; a chunk of trailing rows applies every y_b and ends as
+// the front's update vector.  Both sides: SB rows, 256 / SB threads per row
+// splitting the columns.
 template <class T, class Cv, int SB>
-__global__ void __launch_bounds__(256) k_bwd_block(const SolveBlockTask* __restrict__ tasks, SolveArgs A,
-                                                   const T* __restrict__ panel, const Cv* __restrict__ linv,
-                                                   Cv* __restrict__ fv, Cv* __restrict__ xv) {
-    extern __shared__ __align__(16) unsigned char blk_smem[];
-    Cv* Ls = reinterpret_cast<Cv*>(blk_smem);
-    __shared__ Cv x[SB];
-    __shared__ Cv gn[SB];
-    const SolveBlockTask tk = blocks_or_tasks(tasks);
-    const SnDev d = A.sn[tk.s];
-    const T* P = panel + d.panel_off;
-    const int kn = tk.kn;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
-    const bool next = tk.flags & kSolveNext;
-    if (next) prefetch_inverse<Cv, SB>(Ls, linv + (long long)(tk.blk - 1) * SB * SB);
-    for (int r = 0; r < A.nrhs; ++r) {
-        const long long base = A.fvec_off[tk.s] + r * A.fv_stride;
-        Cv* g = fv + base;
+__global__ void __launch_bounds__(256, 1) k_fwd_level(LevelArgs L, SolveArgs A, const T* __restrict__ panel,
+                                                      const Cv* __restrict__ linv, Cv* fv, Cv* yv,
+                                                      const double* __restrict__ diag, Cv* work) {
+    constexpr int TPR = 256 / SB;   // threads per row
+    constexpr int CPT = SB / TPR;   // columns per thread
+    extern __shared__ __align__(128) unsigned char blk_smem[];
+    // copy destinations aligned to 1024 bytes (the launch adds kLevelSmemSlack)
+    unsigned char* sm = blk_smem + ((1024u - (smem_addr(blk_smem) & 1023u)) & 1023u);
+    T* Tl = reinterpret_cast<T*>(sm);                          // tile L[b+1, b], column-major
+    Cv* Li = reinterpret_cast<Cv*>(sm + SB * SB * sizeof(T));  // inverse of block b+1, column-major
+    __shared__ Cv yb[SB];
+    __shared__ Cv fb[SB];
+    __shared__ Cv part[256];
+    __shared__ int ok;
+    __shared__ unsigned long long tbar;
+    __shared__ unsigned long long sbar[2];
+    const int tid = threadIdx.x, row = tid % SB, pid = tid / SB;
+    if ((int)blockIdx.x < L.nchain_cta) {
+        // tile rows past a partial block are multiplied by zero: start from zeros, not stale bits
+        for (int i = tid; i < SB * SB; i += blockDim.x) {
+            Tl[i] = T(0);
+            Li[i] = Cv(0);
+        }
+        if (tid == 0) bar_init(&tbar);
         __syncthreads();
-        for (int t = threadIdx.x; t < kn; t += blockDim.x) x[t] = xv[base + tk.k0 + t];
-        __syncthreads();
-        for (int c0 = tk.r0 + 4 * warp; c0 < tk.r1; c0 += 4 * nwarps) {
-            Cv acc[4] = {Cv(0), Cv(0), Cv(0), Cv(0)};
-            T vv[4][SB / 32];
-#pragma unroll
-            for (int q = 0; q < 4; ++q)
-#pragma unroll
-                for (int u = 0; u < SB / 32; ++u) {
-                    const int i = lane + 32 * u;
-                    vv[q][u] = (c0 + q < tk.r1 && i < kn) ? P[(long long)(c0 + q) * d.ldp + tk.k0 + i] : T(0);
+        unsigned phase = 0;
+        int q = -1, b = -1;
+        if (!next_chain_duty(L, q, b, 0)) return;
+        // descriptors of the current front, reloaded only when the front changes
+        int cq = -1;
+        SolveBlockTask c;
+        SnDev d;
+        auto front = [&](int qq) {
+            if (qq != cq) {
+                c = L.chains[qq];
+                d = A.sn[c.s];
+                cq = qq;
+            }
+        };
+        auto prefetch = [&](int qq, int bb) {
+            front(qq);
+            const int r0 = (bb + 1) * SB, kn = min(SB, d.w - r0);
+            start_tile_copy<T, Cv, SB>(Tl, Li, L.maps + c.s, r0, bb * SB, bb >= 0,
+                                       linv + (long long)(c.blk + bb + 1) * SB * SB, kn, &tbar);
+        };
+        prefetch(q, b);
+        int held = -1;   // front whose y_b is in yb (single right-hand side)
+        for (;;) {
+            front(q);
+            const int r0 = (b + 1) * SB, kn = min(SB, d.w - r0);
+            // the bulk chunk of block b+1 has applied y_0 .. y_{b-1}
+            if (b >= 1 && !wait_at_least(L.progress + c.k0 + b + 1, b, L.status, &ok)) return;
+            for (int r = 0; r < A.nrhs; ++r) {
+                const long long base = A.fvec_off[c.s] + r * A.fv_stride;
+                const Cv f0 = (pid == 0 && row < kn) ? __ldcg(fv + base + r0 + row) : Cv(0);
+                if (b >= 0 && !(A.nrhs == 1 && held == q)) {
+                    __syncthreads();
+                    for (int t = tid; t < SB; t += blockDim.x) yb[t] = __ldcg(yv + base + b * SB + t);
                 }
-#pragma unroll
-            for (int q = 0; q < 4; ++q)
-#pragma unroll
-                for (int u = 0; u < SB / 32; ++u) {
-                    const int i = lane + 32 * u;
-                    if (i < kn) acc[q] += (Cv)vv[q][u] * x[i];
+                if (r == 0) {
+                    if (!__syncthreads_and(bar_wait(&tbar, phase, L.status))) return;
+                    phase ^= 1;
                 }
+                __syncthreads();
+                // f_{b+1} - L[b+1, b] y_b: thread (row, pid) sums columns [pid CPT, pid CPT + CPT)
+                Cv a4[4] = {Cv(0), Cv(0), Cv(0), Cv(0)};
+                if (b >= 0) {
+#pragma unroll 8
+                    for (int u = 0; u < CPT; ++u) a4[u & 3] += (Cv)Tl[row + (pid * CPT + u) * SB] * yb[pid * CPT + u];
+                }
+                part[tid] = (a4[0] + a4[1]) + (a4[2] + a4[3]);
+                __syncthreads();
+                if (pid == 0) {
+                    Cv v = f0;
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                Cv a = acc[q];
-                for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
-                if (lane == 0 && c0 + q < tk.r1) {
-                    const Cv nv = g[c0 + q] - a;
-                    g[c0 + q] = nv;
-                    if (next) gn[c0 + q - tk.r0] = nv;
+                    for (int p = 0; p < TPR; ++p) v -= part[row + p * SB];
+                    fb[row] = row < kn ? v : Cv(0);
+                }
+                __syncthreads();
+                // y = L_{b+1}^-1 f: thread (row, pid) sums k in [pid CPT, pid CPT + CPT), k <= row
+                Cv s0 = Cv(0), s1 = Cv(0), s2 = Cv(0), s3 = Cv(0);
+                const int kend = min(pid * CPT + CPT, row + 1);
+                int k = pid * CPT;
+                for (; k + 4 <= kend; k += 4) {
+                    s0 += Li[row + k * SB] * fb[k];
+                    s1 += Li[row + (k + 1) * SB] * fb[k + 1];
+                    s2 += Li[row + (k + 2) * SB] * fb[k + 2];
+                    s3 += Li[row + (k + 3) * SB] * fb[k + 3];
+                }
+                for (; k < kend; ++k) s0 += Li[row + k * SB] * fb[k];
+                part[tid] = (s0 + s1) + (s2 + s3);
+                __syncthreads();
+                if (pid == 0 && row < kn) {
+                    Cv y = part[row];
+#pragma unroll
+                    for (int p = 1; p < TPR; ++p) y += part[row + p * SB];
+                    const int col = r0 + row;
+                    yv[base + col] = y;
+                    yb[row] = y;   // y_{b+1}, kept for this front's next duty
+                    work[d.first_col + col + (long long)r * A.ldw] = (Cv)((double)y / diag[d.first_col + col]);
+                } else if (pid == 0) {
+                    yb[row] = Cv(0);
                 }
             }
+            held = q;
+            publish(L.flags + c.blk + b + 1, 1);
+            if (!next_chain_duty(L, q, b, c.kn)) return;
+            prefetch(q, b);
         }
-        if (next) {
-            if (r == 0) cp_async_wait_all();
+    }
+    // ---- bulk CTA: work items (step b, chunk q) in step-major order over its share of the chunks.
+    // Tiles come by tensor-map copies into two stage buffers (the chain's tile and inverse space),
+    // the next item's copy in flight while the current one is applied; the flag and y_b of
+    // consecutive items of one front are shared.
+    const BulkRange R = bulk_range(L);
+    if (R.begin >= R.end || R.step <= 0) return;
+    auto stage = [&](int k) { return k ? reinterpret_cast<T*>(Li) : Tl; };
+    if (tid == 0) {
+        bar_init(&sbar[0]);
+        bar_init(&sbar[1]);
+    }
+    __syncthreads();
+    unsigned phbits = 0;   // expected parity of each stage barrier
+    auto next_item = [&](int& b, int& q) {
+        for (;;) {
+            q = q < 0 ? R.begin : q + R.step;
+            if (q >= R.end) {
+                q = -1;
+                if (++b >= L.steps) return false;
+                continue;
+            }
+            if (b < L.bulk[q].kn) return true;   // kn = the chunk's number of solutions to apply
+        }
+    };
+    // tile rows start at the chunk's first row rounded down to 16 bytes (trailing-row chunks are
+    // SB - 16 / sizeof(T) rows high, so the box still covers them)
+    constexpr int kAlign = 16 / (int)sizeof(T);
+    auto issue = [&](int st_, int b, int q) {
+        if (tid == 0)
+            start_bulk_tile<T, SB>(stage(st_), L.maps + L.bulk[q].s, L.bulk[q].r0 & ~(kAlign - 1), b * SB, &sbar[st_]);
+    };
+    int seen_blk = -1, seen_b = -1, prev_q = -1;
+    Cv fcur = Cv(0);   // f of this thread's row of the previous item (single right-hand side)
+    int b0 = 0, q0 = -1;
+    if (!next_item(b0, q0)) return;
+    int b1 = b0, q1 = q0;
+    bool has1 = next_item(b1, q1);
+    issue(0, b0, q0);
+    if (has1) issue(1, b1, q1);
+    int cur = 0;
+    for (;;) {
+        const SolveBlockTask c = L.bulk[q0];
+        const SnDev d = A.sn[c.s];
+        const int kb = min(SB, d.w - b0 * SB), i = c.r0 + row;
+        const bool same = c.blk == seen_blk && b0 == seen_b;
+        // f of the row, issued before the waits (this thread wrote it last, if anyone did)
+        Cv fold = Cv(0);
+        if (A.nrhs == 1 && pid == 0 && i < c.r1) fold = q0 == prev_q ? fcur : fv[A.fvec_off[c.s] + i];
+        if (!same && !wait_at_least(L.flags + c.blk + b0, 1, L.status, &ok)) return;
+        for (int r = 0; r < A.nrhs; ++r) {
+            const long long base = A.fvec_off[c.s] + r * A.fv_stride;
+            if (!(same && A.nrhs == 1)) {
+                __syncthreads();
+                for (int t = tid; t < SB; t += blockDim.x) yb[t] = t < kb ? __ldcg(yv + base + b0 * SB + t) : Cv(0);
+            }
+            if (r == 0) {
+                if (!__syncthreads_and(bar_wait(&sbar[cur], (phbits >> cur) & 1u, L.status))) return;
+                phbits ^= 1u << cur;
+            }
             __syncthreads();
-            for (int t = warp; t < SB; t += nwarps) {   // the previous block is always full width
-                Cv acc = Cv(0);
-                for (int k = t + lane; k < SB; k += 32) acc += Ls[k + t * SB] * gn[k];
-                for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-                if (lane == 0) xv[base + tk.r0 + t] = acc;
+            const T* tile = stage(cur);
+            const int trow = min(row + (c.r0 & (kAlign - 1)), SB - 1);   // idle rows past the chunk: clamped
+            Cv a4[4] = {Cv(0), Cv(0), Cv(0), Cv(0)};
+#pragma unroll 8
+            for (int u = 0; u < CPT; ++u) a4[u & 3] += (Cv)tile[trow + (pid * CPT + u) * SB] * yb[pid * CPT + u];
+            part[tid] = (a4[0] + a4[1]) + (a4[2] + a4[3]);
+            __syncthreads();
+            if (pid == 0 && i < c.r1) {
+                Cv sum = part[row];
+#pragma unroll
+                for (int p = 1; p < TPR; ++p) sum += part[row + p * SB];
+                const Cv f = (A.nrhs == 1 ? fold : fv[base + i]) - sum;
+                fv[base + i] = f;
+                fcur = f;
             }
         }
+        seen_blk = c.blk;
+        seen_b = b0;
+        prev_q = q0;
+        if (c.r0 < d.w) publish(L.progress + q0, b0 + 1);
+        __syncthreads();   // the stage buffer is free again
+        if (!has1) return;
+        int b2 = b1, q2 = q1;
+        const bool has2 = next_item(b2, q2);
+        if (has2) issue(cur, b2, q2);
+        b0 = b1;
+        q0 = q1;
+        b1 = b2;
+        q1 = q2;
+        has1 = has2;
+        cur ^= 1;
     }
 }
 
-// y = f / D for the supernode's own columns (the diagonal step of the solve).
-template <class Cv>
-__global__ void k_fwd_finish(const SolveBlockTask* __restrict__ tasks, SolveArgs A, const double* __restrict__ diag,
-                             const Cv* __restrict__ fv, Cv* __restrict__ work) {
-    const SolveBlockTask tk = tasks[blockIdx.x];
-    const int s = tk.s;
-    const SnDev d = A.sn[s];
-    for (int r = 0; r < A.nrhs; ++r) {
-        const Cv* f = fv + A.fvec_off[s] + r * A.fv_stride;
-        for (int a = tk.r0 + threadIdx.x; a < tk.r1; a += blockDim.x)
-            work[d.first_col + a + (long long)r * A.ldw] = (Cv)((double)f[a] / diag[d.first_col + a]);
+// Backward.  Chain duty (front, t) for block b = nblk-1-t: x_{b-1} =
+// L_{b-1}^-T (g_{b-1} - L[b, b-1]^T x_b), where the bulk has already applied
+// x_{nblk-1} .. x_{b+1} to g_{b-1} (t = -1 solves the last block from g after
+// the trailing rows' contribution); writes x to the work vector.  Bulk chunk
+// of own columns of block `own` applies x_{nblk-1} .. x_{own+2}
+// (warp-cooperative dots: warp w takes columns 4w + 32p + (0..3), lanes run
+// over the rows of block b).
+template <class T, class Cv, int SB>
+__global__ void __launch_bounds__(256, 1) k_bwd_level(LevelArgs L, SolveArgs A, const T* __restrict__ panel,
+                                                      const Cv* __restrict__ linv, Cv* fv, Cv* xv, Cv* work) {
+    constexpr int NP = SB / 32;   // column passes
+    extern __shared__ __align__(128) unsigned char blk_smem[];
+    unsigned char* sm = blk_smem + ((1024u - (smem_addr(blk_smem) & 1023u)) & 1023u);
+    T* Tl = reinterpret_cast<T*>(sm);                          // tile L[b, b-1], column-major
+    Cv* Li = reinterpret_cast<Cv*>(sm + SB * SB * sizeof(T));  // inverse of block b-1, column-major
+    __shared__ Cv xb[SB];
+    __shared__ Cv gb[SB];
+    __shared__ int ok;
+    __shared__ unsigned long long tbar;
+    __shared__ unsigned long long sbar[2];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, nwarps = blockDim.x >> 5;
+    if ((int)blockIdx.x < L.nchain_cta) {
+        // tile rows past a partial block are multiplied by zero: start from zeros, not stale bits
+        for (int i = tid; i < SB * SB; i += blockDim.x) {
+            Tl[i] = T(0);
+            Li[i] = Cv(0);
+        }
+        if (tid == 0) bar_init(&tbar);
+        __syncthreads();
+        unsigned phase = 0;
+        int q = -1, t = -1;
+        if (!next_chain_duty(L, q, t, 0)) return;
+        int cq = -1;
+        SolveBlockTask c;
+        SnDev d;
+        auto front = [&](int qq) {
+            if (qq != cq) {
+                c = L.chains[qq];
+                d = A.sn[c.s];
+                cq = qq;
+            }
+        };
+        auto prefetch = [&](int qq, int tt) {
+            front(qq);
+            const int bb = c.kn - 1 - tt;   // duty tt solves block bb - 1
+            start_tile_copy<T, Cv, SB>(Tl, Li, L.maps + c.s, bb * SB, (bb - 1) * SB, tt >= 0,
+                                       linv + (long long)(c.blk + bb - 1) * SB * SB, min(SB, d.w - (bb - 1) * SB), &tbar);
+        };
+        prefetch(q, t);
+        int held = -1;   // front whose x_b is in xb (single right-hand side)
+        for (;;) {
+            front(q);
+            const int b = c.kn - 1 - t;                        // x_b is applied (t >= 0)
+            const int tgt = b - 1;                             // block solved by this duty
+            const int c0 = tgt * SB, kn = min(SB, d.w - c0);
+            const int kb = t >= 0 ? min(SB, d.w - b * SB) : 0;  // rows of block b
+            // the bulk chunk of block b-1 has applied x_{nblk-1} .. x_{b+1}
+            if (t >= 1 && !wait_at_least(L.progress + c.k0 + tgt, t, L.status, &ok)) return;
+            for (int r = 0; r < A.nrhs; ++r) {
+                const long long base = A.fvec_off[c.s] + r * A.fv_stride;
+                if (t >= 0 && !(A.nrhs == 1 && held == q)) {
+                    __syncthreads();
+                    for (int i = tid; i < SB; i += blockDim.x) xb[i] = i < kb ? __ldcg(xv + base + b * SB + i) : Cv(0);
+                }
+                if (r == 0) {
+                    if (!__syncthreads_and(bar_wait(&tbar, phase, L.status))) return;
+                    phase ^= 1;
+                }
+                __syncthreads();
+                // g_{b-1} -= L[b, b-1]^T x_b: warp per column of the tile (lanes over its rows)
+                for (int col = warp; col < kn; col += nwarps) {
+                    const Cv g0 = lane == 0 ? __ldcg(fv + base + c0 + col) : Cv(0);
+                    Cv acc = Cv(0);
+                    if (t >= 0) {
+#pragma unroll
+                        for (int u = 0; u < SB / 32; ++u) acc += (Cv)Tl[lane + 32 * u + col * SB] * xb[lane + 32 * u];
+                        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+                    }
+                    if (lane == 0) gb[col] = g0 - acc;
+                }
+                __syncthreads();
+                // x = Li^T g: warp per output column of the inverse
+                for (int tt = warp; tt < kn; tt += nwarps) {
+                    Cv acc = Cv(0);
+                    for (int k = tt + lane; k < kn; k += 32) acc += Li[k + tt * SB] * gb[k];
+                    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+                    if (lane == 0) {
+                        xv[base + c0 + tt] = acc;
+                        xb[tt] = acc;   // x_{b-1}, kept for this front's next duty
+                        work[d.first_col + c0 + tt + (long long)r * A.ldw] = acc;
+                    }
+                }
+                // a partial (last) block: the kept solution is zero past its width, as the tile
+                // rows it meets there hold whatever the copy left
+                for (int i = kn + tid; i < SB; i += blockDim.x) xb[i] = Cv(0);
+            }
+            held = q;
+            publish(L.flags + c.blk + tgt, 1);
+            if (!next_chain_duty(L, q, t, c.kn)) return;
+            prefetch(q, t);
+        }
+    }
+    // ---- bulk CTA: work items (step t, chunk q) over its share of the chunks; tiles by tensor-map
+    // copies into two stage buffers, as in the forward kernel
+    const BulkRange R = bulk_range(L);
+    if (R.begin >= R.end || R.step <= 0) return;
+    auto stage = [&](int k) { return k ? reinterpret_cast<T*>(Li) : Tl; };
+    if (tid == 0) {
+        bar_init(&sbar[0]);
+        bar_init(&sbar[1]);
+    }
+    __syncthreads();
+    unsigned phbits = 0;   // expected parity of each stage barrier
+    auto next_item = [&](int& t, int& q) {
+        for (;;) {
+            q = q < 0 ? R.begin : q + R.step;
+            if (q >= R.end) {
+                q = -1;
+                if (++t >= L.steps) return false;
+                continue;
+            }
+            if (t < L.bulk[q].kn) return true;   // kn = the chunk's number of solutions to apply
+        }
+    };
+    // rows of block b (x), the chunk's columns (y)
+    auto issue = [&](int st_, int t, int q) {
+        if (tid == 0)
+            start_bulk_tile<T, SB>(stage(st_), L.maps + L.bulk[q].s, (L.bulk[q].k0 - t) * SB, L.bulk[q].r0, &sbar[st_]);
+    };
+    int seen_blk = -1, seen_b = -1, prev_q = -1;
+    Cv gcur[NP][4];
+    int t0 = 0, q0 = -1;
+    if (!next_item(t0, q0)) return;
+    int t1 = t0, q1 = q0;
+    bool has1 = next_item(t1, q1);
+    issue(0, t0, q0);
+    if (has1) issue(1, t1, q1);
+    int cur = 0;
+    for (;;) {
+        const SolveBlockTask c = L.bulk[q0];
+        const SnDev d = A.sn[c.s];
+        const int b = c.k0 - t0, kb = min(SB, d.w - b * SB);
+        const bool same = c.blk == seen_blk && b == seen_b;
+        Cv gold[NP][4];
+        if (A.nrhs == 1 && lane == 0) {
+#pragma unroll
+            for (int p = 0; p < NP; ++p)
+#pragma unroll
+                for (int qq = 0; qq < 4; ++qq) {
+                    const int col = c.r0 + 4 * warp + 32 * p + qq;
+                    gold[p][qq] = col < c.r1 ? (q0 == prev_q ? gcur[p][qq] : fv[A.fvec_off[c.s] + col]) : Cv(0);
+                }
+        }
+        if (!same && !wait_at_least(L.flags + c.blk + b, 1, L.status, &ok)) return;
+        for (int r = 0; r < A.nrhs; ++r) {
+            const long long base = A.fvec_off[c.s] + r * A.fv_stride;
+            Cv* g = fv + base;
+            if (!(same && A.nrhs == 1)) {
+                __syncthreads();
+                for (int i = tid; i < SB; i += blockDim.x) xb[i] = i < kb ? __ldcg(xv + base + b * SB + i) : Cv(0);
+            }
+            if (r == 0) {
+                if (!__syncthreads_and(bar_wait(&sbar[cur], (phbits >> cur) & 1u, L.status))) return;
+                phbits ^= 1u << cur;
+            }
+            __syncthreads();
+            const T* tile = stage(cur);
+#pragma unroll
+            for (int p = 0; p < NP; ++p)
+#pragma unroll
+                for (int qq = 0; qq < 4; ++qq) {
+                    const int cl = 4 * warp + 32 * p + qq, col = c.r0 + cl;
+                    Cv a = Cv(0);
+#pragma unroll
+                    for (int u = 0; u < SB / 32; ++u) a += (Cv)tile[lane + 32 * u + cl * SB] * xb[lane + 32 * u];
+                    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+                    if (lane == 0 && col < c.r1) {
+                        const Cv gv = (A.nrhs == 1 ? gold[p][qq] : g[col]) - a;
+                        g[col] = gv;
+                        gcur[p][qq] = gv;
+                    }
+                }
+        }
+        seen_blk = c.blk;
+        seen_b = b;
+        prev_q = q0;
+        publish(L.progress + q0, t0 + 1);
+        __syncthreads();
+        if (!has1) return;
+        int t2 = t1, q2 = q1;
+        const bool has2 = next_item(t2, q2);
+        if (has2) issue(cur, t2, q2);
+        t0 = t1;
+        q0 = q1;
+        t1 = t2;
+        q1 = q2;
+        has1 = has2;
+        cur ^= 1;
     }
 }
 
@@ -344,18 +769,6 @@ __global__ void k_bwd_cols(const SolveBlockTask* __restrict__ tasks, SolveArgs A
         for (int i = tk.r0 + lane; i < tk.r1; i += 32) acc += (Cv)col[i] * g[i];
         for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
         if (lane == 0) g[k] -= acc;
-    }
-}
-
-template <class Cv>
-__global__ void k_bwd_finish(const SolveBlockTask* __restrict__ tasks, SolveArgs A, const Cv* __restrict__ fv,
-                             Cv* __restrict__ work) {
-    const SolveBlockTask tk = tasks[blockIdx.x];
-    const int s = tk.s;
-    const SnDev d = A.sn[s];
-    for (int r = 0; r < A.nrhs; ++r) {
-        const Cv* g = fv + A.fvec_off[s] + r * A.fv_stride;
-        for (int a = tk.r0 + threadIdx.x; a < tk.r1; a += blockDim.x) work[d.first_col + a + (long long)r * A.ldw] = g[a];
     }
 }
 
