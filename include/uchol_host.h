@@ -109,6 +109,20 @@ void uchol_analysis_destroy(uchol_analysis a);
 
 /* Individual symbolic steps, exposed for parity tests against the
  * reference's own unit tests (AMD permutation validity, etc.). */
+/* Batches of independent systems (many small problems at once; no counterpart in the
+ * reference, whose solvers take one SymmetricCSRMatrix per call): the block-diagonal
+ * union of `count` upper-CSR systems, system q occupying rows and columns
+ * [sum_{p<q} sizes[p], ...).  uchol_batch_csr builds the union matrix (values in the
+ * systems' CSR order, concatenated).  uchol_batch_analyze orders every system on its
+ * own (the reference's AMD or natural order, as UtduSymbolicFactorization.Analyze does
+ * for one matrix) and analyses the union with that order: the elimination forest has
+ * one tree per system, each with the supernodes of that system's own analysis, so one
+ * numeric factorisation and one solve of the union treat every system in each launch. */
+int uchol_batch_csr(int count, const int* sizes, const int* const* row_ptrs, const int* const* cols,
+                    const double* const* values, uchol_csr* out);
+int uchol_batch_analyze(int count, const int* sizes, const int* const* row_ptrs, const int* const* cols, int ordering,
+                        int amalgamation_limit, uchol_analysis* out);
+
 int uchol_amd_order(int n, const int* row_ptr, const int* col, int* perm_out);
 
 const char* uchol_host_last_error(void);

@@ -8,13 +8,15 @@ from .errors import (ArgumentException, ArgumentNullException, ArgumentOutOfRang
                      DeviceWaitTimeoutError, IndexOutOfRangeException, InvalidOperationException,
                      RefinementNotConvergedError)
 from .matrix import LinearSystem, MatrixEntry, SymmetricCSRMatrix, SymmetricCSRMatrixBuilder
-from .solver import (DirectLinearSolver, FillReducingOrdering, LinearSolver, Precision, ResidualCalculator,
-                     SymmetricUtduSolver, UtduNumericFactorization, UtduSolverOptions, UtduSymbolicFactorization)
+from .solver import (BatchedUtduFactorization, BatchedUtduSolver, BatchedUtduSymbolic, DirectLinearSolver,
+                     FillReducingOrdering, LinearSolver, Precision, ResidualCalculator, SymmetricUtduSolver,
+                     UtduNumericFactorization, UtduSolverOptions, UtduSymbolicFactorization)
 
 __all__ = [
     "ArgumentException", "ArgumentNullException", "ArgumentOutOfRangeException", "DeviceOutOfMemoryError",
     "DeviceWaitTimeoutError", "IndexOutOfRangeException", "InvalidOperationException", "RefinementNotConvergedError",
     "LinearSystem", "MatrixEntry", "SymmetricCSRMatrix", "SymmetricCSRMatrixBuilder", "DirectLinearSolver",
-    "FillReducingOrdering", "LinearSolver", "Precision", "ResidualCalculator", "SymmetricUtduSolver",
-    "UtduNumericFactorization", "UtduSolverOptions", "UtduSymbolicFactorization",
+    "BatchedUtduFactorization", "BatchedUtduSolver", "BatchedUtduSymbolic", "FillReducingOrdering", "LinearSolver",
+    "Precision", "ResidualCalculator", "SymmetricUtduSolver", "UtduNumericFactorization", "UtduSolverOptions",
+    "UtduSymbolicFactorization",
 ]

@@ -105,6 +105,10 @@ HOST_SYMBOLS = {
     "uchol_analysis_copy": (C.c_int, [C.c_void_p, C.c_int, c_int_p]),
     "uchol_analysis_destroy": (None, [C.c_void_p]),
     "uchol_amd_order": (C.c_int, [C.c_int, c_int_p, c_int_p, c_int_p]),
+    "uchol_batch_csr": (C.c_int, [C.c_int, c_int_p, C.POINTER(c_int_p), C.POINTER(c_int_p), C.POINTER(c_double_p),
+                                  c_void_pp]),
+    "uchol_batch_analyze": (C.c_int, [C.c_int, c_int_p, C.POINTER(c_int_p), C.POINTER(c_int_p), C.c_int, C.c_int,
+                                      c_void_pp]),
     "uchol_host_last_error": (C.c_char_p, []),
 }
 

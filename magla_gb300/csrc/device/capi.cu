@@ -111,7 +111,7 @@ struct DBuf {
 
 struct DevPlan {
     Plan plan;
-    DBuf sn, rel, asm_pos, zero_off, zero_len, ea_items, ea_entries, small, pivot_tasks, panel_tasks, simt_jobs, tc_jobs,
+    DBuf sn, rel, asm_pos, ea_items, ea_entries, small, pivot_tasks, panel_tasks, simt_jobs, tc_jobs,
         stage;
     DBuf fvec_off, solve_fronts, solve_tasks, inv_blocks;
 };
@@ -154,8 +154,6 @@ struct uchol_symbolic_s {
         dp->sn.upload(P.sn, stream, "supernode table");
         dp->rel.upload(P.rel, stream, "relative indices");
         dp->asm_pos.upload(P.assemble_pos, stream, "assembly map");
-        dp->zero_off.upload(P.zero_off, stream, "plan");
-        dp->zero_len.upload(P.zero_len, stream, "plan");
         dp->ea_items.upload(P.ea_items, stream, "plan");
         dp->ea_entries.upload(P.ea_entries, stream, "plan");
         dp->small.upload(P.small_fronts, stream, "plan");
@@ -274,12 +272,6 @@ void run_factor_launches(uchol_factor_s* F, cudaStream_t st) {
             ev_kind.push_back((int)L.kind);
         }
         switch (L.kind) {
-            case Launch::ZeroContrib: {
-                dim3 g(64, std::min(L.count, 65535));
-                k_zero_ranges<T><<<g, 256, 0, st>>>(D.zero_off.as<long long>() + L.begin,
-                                                     D.zero_len.as<long long>() + L.begin, L.count, contrib);
-                break;
-            }
             case Launch::ExtendAdd:
                 k_extend_add<T><<<(L.count + 7) / 8, 256, 0, st>>>(D.ea_items.as<EaItem>() + L.begin, L.count,
                                                                    D.ea_entries.as<EaEntry>(), sn, D.rel.as<int>(),
@@ -354,7 +346,7 @@ void run_factor_launches(uchol_factor_s* F, cudaStream_t st) {
             cudaEventDestroy(ev[q].first);
             cudaEventDestroy(ev[q].second);
         }
-        F->phases.extend_add_ms = sum[Launch::ExtendAdd] + sum[Launch::ZeroContrib];
+        F->phases.extend_add_ms = sum[Launch::ExtendAdd];
         F->phases.small_fronts_ms = sum[Launch::SmallFronts];
         F->phases.panel_ms = sum[Launch::PivotBlock] + sum[Launch::Trsm] + sum[Launch::DiagBlock] + sum[Launch::PanelSolve];
         F->phases.schur_ms = sum[Launch::SimtUpdate] + sum[Launch::TcUpdate];

@@ -85,19 +85,12 @@ __global__ void k_assemble(const double* __restrict__ values, const long long* _
         panel[pos[k]] = (T)values[k];
 }
 
-template <class T>
-__global__ void k_zero_ranges(const long long* __restrict__ off, const long long* __restrict__ len, int count,
-                              T* __restrict__ arena) {
-    for (int r = blockIdx.y; r < count; r += gridDim.y) {
-        long long o = off[r], l = len[r];
-        for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < l; k += (long long)gridDim.x * blockDim.x)
-            arena[o + k] = T(0);
-    }
-}
-
 // Extend-add: one warp per receiving parent column; the children's columns
 // that land in it are added in child order (deterministic, no atomics).
-// UtduNumericFactorization.cs:471-509.
+// UtduNumericFactorization.cs:471-509.  A column of the parent's contribution
+// block is first cleared from its diagonal down (the reference zeroes the
+// whole front, :441-447; only the lower triangle is ever read), so the
+// clearing costs no pass of its own and the adds find the lines in L2.
 template <class T>
 __global__ void k_extend_add(const EaItem* __restrict__ items, int count, const EaEntry* __restrict__ entries,
                              const SnDev* __restrict__ sn, const int* __restrict__ rel, T* __restrict__ panel,
@@ -113,8 +106,17 @@ __global__ void k_extend_add(const EaItem* __restrict__ items, int count, const 
         dst = panel + P.panel_off + (long long)it.pcol * P.ldp;
         shift = 0;
     } else {
-        dst = contrib + P.contrib_off + (long long)(it.pcol - P.w) * P.ldc;
+        const int c = it.pcol - P.w, t = P.m - P.w;
+        dst = contrib + P.contrib_off + (long long)c * P.ldc;
         shift = P.w;
+        // rows [c, t): 16-byte stores between a scalar head and tail (the column starts on a
+        // 16-byte boundary: contribution offsets are multiples of 64 elements, ldc of 8)
+        constexpr int V = 16 / (int)sizeof(T);
+        const int head = min(t, (c + V - 1) / V * V), body = max(head, t / V * V);
+        for (int r = c + lane; r < head; r += 32) dst[r] = T(0);
+        for (int v = head / V + lane; v < body / V; v += 32) reinterpret_cast<uint4*>(dst)[v] = make_uint4(0u, 0u, 0u, 0u);
+        for (int r = body + lane; r < t; r += 32) dst[r] = T(0);
+        __syncwarp();
     }
     for (int e = it.begin; e < it.end; ++e) {
         const EaEntry en = entries[e];

@@ -234,17 +234,6 @@ Plan build_plan(int n, int count, const int* first_column, const int* parent, co
     const int TS = cfg.tile;
     for (int L = 0; L < P.levels; ++L) {
         const auto& fronts = at_level[L];
-        // clear contribution blocks of this level
-        int zb = (int)P.zero_off.size();
-        for (int s : fronts) {
-            const SnDev& d = P.sn[s];
-            if (d.m > d.w) {
-                P.zero_off.push_back(d.contrib_off);
-                P.zero_len.push_back((long long)d.ldc * (d.m - d.w));
-            }
-        }
-        if ((int)P.zero_off.size() > zb) P.launches.push_back({Launch::ZeroContrib, zb, (int)P.zero_off.size() - zb, 0});
-
         // extend-add: one item per receiving parent column
         int ib = (int)P.ea_items.size();
         for (int s : fronts) {
@@ -259,13 +248,20 @@ Plan build_plan(int n, int count, const int* first_column, const int* parent, co
             std::stable_sort(recs.begin(), recs.end(), [](const Rec& x, const Rec& y) {
                 return x.pcol != y.pcol ? x.pcol < y.pcol : x.order < y.order;
             });
+            // panel columns that receive entries, then every contribution column (its item also
+            // clears the column's lower part before adding, so no separate clearing pass exists)
+            const SnDev& pd = P.sn[s];
             size_t q = 0;
-            while (q < recs.size()) {
-                EaItem it;
-                it.parent = s;
-                it.pcol = recs[q].pcol;
-                it.begin = (int)P.ea_entries.size();
-                for (; q < recs.size() && recs[q].pcol == it.pcol; ++q) P.ea_entries.push_back({recs[q].child, recs[q].a});
+            while (q < recs.size() && recs[q].pcol < pd.w) {
+                EaItem it{s, recs[q].pcol, (int)P.ea_entries.size(), 0};
+                for (const int pc = it.pcol; q < recs.size() && recs[q].pcol == pc; ++q)
+                    P.ea_entries.push_back({recs[q].child, recs[q].a});
+                it.end = (int)P.ea_entries.size();
+                P.ea_items.push_back(it);
+            }
+            for (int pc = pd.w; pc < pd.m; ++pc) {
+                EaItem it{s, pc, (int)P.ea_entries.size(), 0};
+                for (; q < recs.size() && recs[q].pcol == pc; ++q) P.ea_entries.push_back({recs[q].child, recs[q].a});
                 it.end = (int)P.ea_entries.size();
                 P.ea_items.push_back(it);
             }

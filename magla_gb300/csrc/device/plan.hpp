@@ -28,7 +28,7 @@ struct PlanConfig {
 // One kernel launch: a contiguous range of tasks in one of the task arrays.
 struct Launch {
     enum Kind : int {
-        ZeroContrib, ExtendAdd, SmallFronts, PivotBlock, Trsm, SimtUpdate, TcUpdate, DiagBlock, PanelSolve,
+        ExtendAdd, SmallFronts, PivotBlock, Trsm, SimtUpdate, TcUpdate, DiagBlock, PanelSolve,
         KindCount
     } kind;
     int begin, count;   // task range
@@ -81,7 +81,6 @@ struct Plan {
     std::vector<long long> fvec_off;           // per supernode offset into the front-vector workspace
 
     // factorisation tasks
-    std::vector<long long> zero_off, zero_len;   // contribution blocks cleared before extend-add
     std::vector<EaItem> ea_items;
     std::vector<EaEntry> ea_entries;
     std::vector<int> small_fronts;

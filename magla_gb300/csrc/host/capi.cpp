@@ -1,4 +1,5 @@
 // C-ABI of the host half (include/uchol_host.h).
+#include <cstdint>
 #include <cstring>
 #include <exception>
 #include <string>
@@ -196,6 +197,102 @@ int uchol_analysis_copy(uchol_analysis a, int which, int* out) {
 }
 
 void uchol_analysis_destroy(uchol_analysis a) { delete a; }
+
+// Validates one upper-CSR system of a batch.
+static void check_upper(int n, const int* row_ptr, const int* col) {
+    if (n < 0 || (n > 0 && (!row_ptr || !col))) throw std::invalid_argument("null or negative argument in a batch system");
+    if (n > 0 && row_ptr[0] != 0) throw std::invalid_argument("row pointers of a batch system do not start at 0");
+    for (int r = 0; r < n; ++r) {
+        if (row_ptr[r + 1] < row_ptr[r]) throw std::invalid_argument("row pointers are not monotone");
+        for (int k = row_ptr[r]; k < row_ptr[r + 1]; ++k) {
+            if (col[k] < r || col[k] >= n) throw std::out_of_range("column index outside the upper triangle");
+            if (k > row_ptr[r] && col[k] <= col[k - 1]) throw std::invalid_argument("columns not strictly ascending");
+        }
+    }
+}
+
+int uchol_batch_csr(int count, const int* sizes, const int* const* row_ptrs, const int* const* cols,
+                    const double* const* values, uchol_csr* out) {
+    return guarded([&] {
+        if (!out || count < 0 || (count > 0 && (!sizes || !row_ptrs || !cols || !values)))
+            throw std::invalid_argument("null or negative argument");
+        uchol::UpperCsr m;
+        int64_t n = 0, nnz = 0;
+        for (int q = 0; q < count; ++q) {
+            check_upper(sizes[q], row_ptrs[q], cols[q]);
+            if (sizes[q] > 0 && !values[q]) throw std::invalid_argument("null values of a batch system");
+            n += sizes[q];
+            nnz += sizes[q] > 0 ? row_ptrs[q][sizes[q]] : 0;
+        }
+        if (n > INT32_MAX || nnz > INT32_MAX) throw std::length_error("the batch exceeds the 32-bit index range");
+        m.n = (int)n;
+        m.row_ptr.reserve(n + 1);
+        m.row_ptr.push_back(0);
+        m.col.reserve(nnz);
+        m.val.reserve(nnz);
+        m.diag_index.assign(n, -1);
+        int off = 0;
+        for (int q = 0; q < count; ++q) {
+            const int nq = sizes[q];
+            for (int r = 0; r < nq; ++r) {
+                for (int k = row_ptrs[q][r]; k < row_ptrs[q][r + 1]; ++k) {
+                    if (cols[q][k] == r) m.diag_index[off + r] = (int)m.col.size();
+                    m.col.push_back(off + cols[q][k]);
+                    m.val.push_back(values[q][k]);
+                }
+                m.row_ptr.push_back((int)m.col.size());
+            }
+            off += nq;
+        }
+        *out = new uchol_csr_s{std::move(m)};
+    });
+}
+
+int uchol_batch_analyze(int count, const int* sizes, const int* const* row_ptrs, const int* const* cols, int ordering,
+                        int amalgamation_limit, uchol_analysis* out) {
+    return guarded([&] {
+        if (!out || count < 0 || (count > 0 && (!sizes || !row_ptrs || !cols)))
+            throw std::invalid_argument("null or negative argument");
+        if (ordering != UCHOL_ORDERING_NATURAL && ordering != UCHOL_ORDERING_AMD)
+            throw std::invalid_argument("unknown ordering");
+        int64_t n = 0, nnz = 0;
+        for (int q = 0; q < count; ++q) {
+            check_upper(sizes[q], row_ptrs[q], cols[q]);
+            n += sizes[q];
+            nnz += sizes[q] > 0 ? row_ptrs[q][sizes[q]] : 0;
+        }
+        if (n > INT32_MAX || nnz > INT32_MAX) throw std::length_error("the batch exceeds the 32-bit index range");
+        // the union's pattern, and each system's own fill-reducing order shifted to its rows
+        std::vector<int> rp, cl, order;
+        rp.reserve(n + 1);
+        rp.push_back(0);
+        cl.reserve(nnz);
+        order.reserve(n);
+        int off = 0;
+        for (int q = 0; q < count; ++q) {
+            const int nq = sizes[q];
+            for (int r = 0; r < nq; ++r) {
+                for (int k = row_ptrs[q][r]; k < row_ptrs[q][r + 1]; ++k) cl.push_back(off + cols[q][k]);
+                rp.push_back((int)cl.size());
+            }
+            if (ordering == UCHOL_ORDERING_AMD) {
+                auto p = uchol::amd_order(uchol::adjacency_from_upper(nq, row_ptrs[q], cols[q]));
+                for (int v : p) order.push_back(off + v);
+            } else {
+                for (int v = 0; v < nq; ++v) order.push_back(off + v);
+            }
+            off += nq;
+        }
+        auto a = new uchol_analysis_s;
+        try {
+            a->s = uchol::analyze_ordered((int)n, rp.data(), cl.data(), (int)nnz, order, amalgamation_limit);
+        } catch (...) {
+            delete a;
+            throw;
+        }
+        *out = a;
+    });
+}
 
 int uchol_amd_order(int n, const int* row_ptr, const int* col, int* perm_out) {
     return guarded([&] {

@@ -349,9 +349,6 @@ FactorLayout build_layout(const Supernodes& sn) {
 
 // UtduSymbolicFactorization.cs:240-295.
 Symbolic analyze(int n, const int* row_ptr, const int* col, int nnz, Ordering ordering, int amalgamation_limit) {
-    Symbolic S;
-    S.n = n;
-    S.matrix_nonzero_count = nnz;
     std::vector<int> fill_reducing(n);
     if (ordering == Ordering::ApproximateMinimumDegree) {
         AdjacencyGraph g = adjacency_from_upper(n, row_ptr, col);
@@ -359,6 +356,16 @@ Symbolic analyze(int n, const int* row_ptr, const int* col, int nnz, Ordering or
     } else {
         std::iota(fill_reducing.begin(), fill_reducing.end(), 0);
     }
+    return analyze_ordered(n, row_ptr, col, nnz, fill_reducing, amalgamation_limit);
+}
+
+// The same analysis from a given fill-reducing order (position -> original index).
+Symbolic analyze_ordered(int n, const int* row_ptr, const int* col, int nnz, const std::vector<int>& fill_reducing,
+                         int amalgamation_limit) {
+    Symbolic S;
+    S.n = n;
+    S.matrix_nonzero_count = nnz;
+    if ((int)fill_reducing.size() != n) throw std::invalid_argument("ordering length does not match the matrix size");
     // Postorder the elimination tree of the ordered matrix so that every
     // supernode and every subtree occupies a contiguous column range.
     std::vector<int> first_inv = invert(fill_reducing);

@@ -109,5 +109,9 @@ struct Symbolic {
 };
 
 Symbolic analyze(int n, const int* row_ptr, const int* col, int nnz, Ordering ordering, int amalgamation_limit);
+// The analysis from a given fill-reducing order (position -> original index), e.g. one AMD
+// ordering per diagonal block of a block-diagonal system.
+Symbolic analyze_ordered(int n, const int* row_ptr, const int* col, int nnz, const std::vector<int>& fill_reducing,
+                         int amalgamation_limit);
 
 }  // namespace uchol

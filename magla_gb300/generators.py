@@ -31,9 +31,27 @@ def laplacian3d(nx: int, ny: int, nz: int) -> SymmetricCSRMatrix:
 
 
 def laplacian2d(n: int, stencil: int = 5, shift=None) -> SymmetricCSRMatrix:
+    """2D Laplacian on an n x n grid (5- or 9-point stencil, Dirichlet boundary
+    eliminated); ``shift`` (a scalar or one value per node) is added to the diagonal."""
+    if stencil not in (5, 9):
+        raise ValueError("stencil must be 5 or 9")
     h = C.c_void_p()
-    s = None if shift is None else np.ascontiguousarray(shift, np.float64)
+    s = None
+    if shift is not None:
+        s = np.ascontiguousarray(np.broadcast_to(np.asarray(shift, np.float64), (n * n,)))
     return _adopt(_native.host().uchol_csr_laplacian2d(n, stencil, _native.ptr(s, C.c_double), C.byref(h)), h)
+
+
+def laplacian2d_batch(count: int = 256, seed: int = 4, n_range=(16, 128)):
+    """Independent 2D Laplacian systems: grid edge n uniform in n_range, 5- or
+    9-point stencil chosen at random, diagonal plus uniform[0, 0.1] per node."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        n = int(rng.integers(n_range[0], n_range[1] + 1))
+        stencil = 5 if rng.random() < 0.5 else 9
+        out.append(laplacian2d(n, stencil, rng.uniform(0.0, 0.1, n * n)))
+    return out
 
 
 def elasticity(ex: int, ey: int, ez: int, youngs=None, nu: float = 0.3, clamp: bool = True):

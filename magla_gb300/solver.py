@@ -107,6 +107,12 @@ class UtduSymbolicFactorization:
                                _native.ptr(matrix.ColumnIndices), int(options.Ordering),
                                max(1, int(options.SupernodeAmalgamationLimit)), C.byref(h))
         raise_for_status(st, lib.uchol_host_last_error())
+        return cls._from_analysis(h, matrix)
+
+    @classmethod
+    def _from_analysis(cls, h, matrix: SymmetricCSRMatrix) -> "UtduSymbolicFactorization":
+        """Takes over an analysis handle of the host library (and destroys it)."""
+        lib = _native.host()
         self = cls.__new__(cls)
         try:
             info = _native.AnalysisInfo()
@@ -507,6 +513,144 @@ class SymmetricUtduSolver(DirectLinearSolver):
 
     def SolveCore(self, matrix, right_hand_side):
         return self.Factorize(matrix).Solve(right_hand_side)
+
+
+class BatchedUtduSolver:
+    """Many independent systems factorised and solved together.
+
+    The systems form the diagonal blocks of one union matrix.  Each is ordered
+    on its own (the options' ordering), and the union is analysed with that
+    order, so the elimination forest holds one tree per system with that
+    system's own supernodes; every kernel launch of the factorisation and of
+    the solves then works on all systems at once.  The reference has no batch
+    entry point (its solvers take one ``SymmetricCSRMatrix`` per call); each
+    system's factor and solution are those of solving it alone, up to the
+    order of floating-point sums.
+    """
+
+    def __init__(self, options: UtduSolverOptions | None = None):
+        self.Options = options if options is not None else UtduSolverOptions()
+
+    @staticmethod
+    def _arrays(matrices):
+        if matrices is None:
+            raise ArgumentNullException("matrices")
+        mats = list(matrices)
+        if any(m is None for m in mats):
+            raise ArgumentNullException("matrices")
+        sizes = np.array([m.Size for m in mats], np.int32)
+        rp = [np.ascontiguousarray(m.RowPointers, np.int32) for m in mats]
+        cl = [np.ascontiguousarray(m.ColumnIndices, np.int32) for m in mats]
+        return mats, sizes, rp, cl
+
+    @staticmethod
+    def _ptrs(arrays, ctype):
+        P = C.POINTER(ctype)
+        return (P * max(1, len(arrays)))(*[a.ctypes.data_as(P) for a in arrays])
+
+    def Union(self, matrices) -> SymmetricCSRMatrix:
+        """The block-diagonal union of the systems (values in the systems' order)."""
+        mats, sizes, rp, cl = self._arrays(matrices)
+        vals = [np.ascontiguousarray(m.Values, np.float64) for m in mats]
+        lib = _native.host()
+        h = C.c_void_p()
+        st = lib.uchol_batch_csr(len(mats), _native.ptr(sizes), self._ptrs(rp, C.c_int), self._ptrs(cl, C.c_int),
+                                 self._ptrs(vals, C.c_double), C.byref(h))
+        raise_for_status(st, lib.uchol_host_last_error())
+        return SymmetricCSRMatrix._from_handle(h)
+
+    def Analyze(self, matrices) -> "BatchedUtduSymbolic":
+        mats, sizes, rp, cl = self._arrays(matrices)
+        lib = _native.host()
+        h = C.c_void_p()
+        st = lib.uchol_batch_analyze(len(mats), _native.ptr(sizes), self._ptrs(rp, C.c_int), self._ptrs(cl, C.c_int),
+                                     int(self.Options.Ordering), max(1, int(self.Options.SupernodeAmalgamationLimit)),
+                                     C.byref(h))
+        raise_for_status(st, lib.uchol_host_last_error())
+        union = self.Union(mats)
+        return BatchedUtduSymbolic(UtduSymbolicFactorization._from_analysis(h, union), sizes)
+
+    def Factorize(self, matrices, symbolic: "BatchedUtduSymbolic | None" = None) -> "BatchedUtduFactorization":
+        mats = list(matrices)
+        if symbolic is None:
+            symbolic = self.Analyze(mats)
+        elif len(mats) != len(symbolic.Sizes) or any(m.Size != n for m, n in zip(mats, symbolic.Sizes)):
+            raise ArgumentException("The systems do not match the batch analysis.")
+        union = self.Union(mats)
+        f = SymmetricUtduSolver(self.Options).Factorize(union, symbolic.Union)
+        return BatchedUtduFactorization(f, symbolic, self.Options)
+
+
+class BatchedUtduSymbolic:
+    """Analysis of a batch: the union's symbolic factorisation and the system sizes."""
+
+    def __init__(self, union: UtduSymbolicFactorization, sizes):
+        self.Union = union
+        self.Sizes = np.asarray(sizes, np.int64)
+        self.Offsets = np.concatenate([[0], np.cumsum(self.Sizes)]).astype(np.int64)
+
+    @property
+    def Count(self) -> int:
+        return len(self.Sizes)
+
+    @property
+    def FactorOperationCount(self) -> int:
+        return self.Union.FactorOperationCount
+
+
+class BatchedUtduFactorization:
+    """Factor of a batch; ``Solve`` takes one right-hand side (vector or n_q x k block) per system."""
+
+    def __init__(self, union_factor: UtduNumericFactorization, symbolic: BatchedUtduSymbolic, options):
+        self.Union = union_factor
+        self.Symbolic = symbolic
+        self._options = options
+
+    def _stack(self, right_hand_sides):
+        if right_hand_sides is None:
+            raise ArgumentNullException("rightHandSides")
+        bs = [np.asarray(b, np.float64) for b in right_hand_sides]
+        S = self.Symbolic
+        if len(bs) != S.Count:
+            raise ArgumentException(f"{len(bs)} right-hand sides for {S.Count} systems.")
+        k = bs[0].shape[1] if bs and bs[0].ndim == 2 else 1
+        B = np.zeros((int(S.Offsets[-1]), k))
+        for q, b in enumerate(bs):
+            if b.shape[0] != S.Sizes[q] or (b.ndim == 2 and b.shape[1] != k) or (b.ndim == 1 and k != 1):
+                raise ArgumentException(f"The right-hand side of system {q} does not match its size.")
+            B[S.Offsets[q]:S.Offsets[q + 1]] = b.reshape(b.shape[0], -1)
+        return bs, B
+
+    def _split(self, X, bs):
+        S = self.Symbolic
+        return [X[S.Offsets[q]:S.Offsets[q + 1]].reshape(bs[q].shape) for q in range(S.Count)]
+
+    def Solve(self, right_hand_sides):
+        """Solutions of every system.  A mixed-precision factor is refined until the
+        relative residual of every column of every system reaches the tolerance: the
+        columns are scaled to unit norm per system and the union is refined to
+        tolerance / sqrt(systems)."""
+        bs, B = self._stack(right_hand_sides)
+        if self.Union.Precision == Precision.FP64:
+            return self._split(self.Union._apply(B), bs)
+        S = self.Symbolic
+        scale = np.ones((S.Count, B.shape[1]))
+        for q in range(S.Count):
+            blk = B[S.Offsets[q]:S.Offsets[q + 1]]
+            nrm = np.linalg.norm(blk, axis=0)
+            scale[q] = np.where(nrm > 0, nrm, 1.0)
+            B[S.Offsets[q]:S.Offsets[q + 1]] = blk / scale[q]
+        tol = self._options.RefinementTolerance / np.sqrt(max(1, S.Count))
+        X = self.Union.SolveRefined(B, tol, self._options.RefinementMaxIterations).reshape(B.shape)
+        for q in range(S.Count):
+            X[S.Offsets[q]:S.Offsets[q + 1]] *= scale[q]
+        return self._split(X, bs)
+
+    def Refactorize(self, matrices) -> None:
+        mats = list(matrices)
+        if len(mats) != self.Symbolic.Count:
+            raise ArgumentException("The systems do not match the batch analysis.")
+        self.Union.Refactorize(BatchedUtduSolver(self._options).Union(mats))
 
 
 class ResidualCalculator:
