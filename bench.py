@@ -160,6 +160,7 @@ def run_ours(args):
     import torch
     import magla_gb300 as mg
     from magla_gb300 import _native
+    from magla_gb300.replicas import max_over_ranks
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -208,11 +209,7 @@ def run_ours(args):
         ev1.record(stream)
         torch.cuda.synchronize()
     launches = lib.uchol_kernel_launches() - launches0
-    ms = ev0.elapsed_time(ev1) / args.steps
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ev0.elapsed_time(ev1) / args.steps)   # replicas: the slowest rank defines the step
     relres = f.DeviceResidualNorms(b, d_x.cpu().numpy())[0] / np.linalg.norm(b)
 
     # end to end through the public API with host buffers

@@ -124,6 +124,9 @@ inline int grid_for(long long work, int block, int cap = 152 * 16) {
 }  // namespace
 
 struct uchol_symbolic_s {
+    // held by its handle and by every factor made from it: the caller may destroy the handle
+    // before its factors (a garbage collector picks any order), the object outlives them
+    std::atomic<int> refs{1};
     int device = 0;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
@@ -193,17 +196,30 @@ struct uchol_factor_s {
     int solve_graph_nrhs = 0, solve_graph_nodes = 0;
     cudaGraphExec_t factor_graph = nullptr;
     int factor_graph_nodes = 0;
-    ~uchol_factor_s() {
-        if (solve_graph) cudaGraphExecDestroy(solve_graph);
-        if (factor_graph) cudaGraphExecDestroy(factor_graph);
-        if (capture_stream) cudaStreamDestroy(capture_stream);
-    }
+    ~uchol_factor_s();
     DBuf maps;                    // tensor-map pairs of the staging regions
     int sms = 148;
     uchol_factor_stats last{};
     uchol_phase_times phases{};
     std::mutex mu;
 };
+
+// Drops one reference; the last one frees the symbolic object and its own stream.
+void symbolic_release(uchol_symbolic_s* s) {
+    if (s->refs.fetch_sub(1) != 1) return;
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    cudaStream_t st = s->stream;
+    const bool own = s->own_stream;
+    delete s;
+    if (own && st) cudaStreamDestroy(st);
+}
+
+uchol_factor_s::~uchol_factor_s() {
+    if (solve_graph) cudaGraphExecDestroy(solve_graph);
+    if (factor_graph) cudaGraphExecDestroy(factor_graph);
+    if (capture_stream) cudaStreamDestroy(capture_stream);
+    if (sym) symbolic_release(sym);
+}
 
 namespace {
 
@@ -541,6 +557,7 @@ uchol_factor_s* create_factor(uchol_symbolic_s* S, int n, int nnz, const uchol_o
     check_options(opts);
     auto F = std::make_unique<uchol_factor_s>();
     F->sym = S;
+    S->refs.fetch_add(1);
     if (opts) F->opts = *opts; else uchol_default_options(&F->opts);
     F->precision = F->opts.precision;
     F->elem = F->precision == UCHOL_PRECISION_FP64 ? 8 : 4;
@@ -1069,12 +1086,7 @@ int uchol_estimate_device_bytes(const uchol_symbolic_desc* d, const uchol_option
 
 int uchol_symbolic_destroy(uchol_symbolic s) {
     return guarded([&] {
-        if (!s) return;
-        if (s->stream) cudaStreamSynchronize(s->stream);
-        cudaStream_t st = s->stream;
-        bool own = s->own_stream;
-        delete s;
-        if (own && st) cudaStreamDestroy(st);
+        if (s) symbolic_release(s);
     });
 }
 

@@ -125,19 +125,20 @@ __global__ void k_extend_add(const EaItem* __restrict__ items, int count, const 
         const int* r = rel + C.rel_off;
         const T* src = contrib + C.contrib_off + (long long)en.a * C.ldc;
         // rows of one child column are distinct, so loads of a batch are issued before its stores
-        for (int b0 = en.a + lane; b0 < t; b0 += 32 * 4) {
-            int idx[4];
-            T sv[4], dv[4];
+        constexpr int D = 8;   // loads of a batch in flight per lane
+        for (int b0 = en.a + lane; b0 < t; b0 += 32 * D) {
+            int idx[D];
+            T sv[D], dv[D];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
+            for (int u = 0; u < D; ++u) {
                 const int b = b0 + 32 * u;
                 idx[u] = b < t ? r[b] - shift : -1;
                 sv[u] = b < t ? src[b] : T(0);
             }
 #pragma unroll
-            for (int u = 0; u < 4; ++u) dv[u] = idx[u] >= 0 ? dst[idx[u]] : T(0);
+            for (int u = 0; u < D; ++u) dv[u] = idx[u] >= 0 ? dst[idx[u]] : T(0);
 #pragma unroll
-            for (int u = 0; u < 4; ++u)
+            for (int u = 0; u < D; ++u)
                 if (idx[u] >= 0) dst[idx[u]] = dv[u] + sv[u];
         }
         __syncwarp();

@@ -13,6 +13,8 @@
 
 #include <cuda.h>
 
+#include <type_traits>
+
 #include "common.cuh"
 #include "plan.hpp"
 
@@ -754,19 +756,48 @@ __global__ void k_bwd_gather(const SolveBlockTask* __restrict__ tasks, SolveArgs
 }
 
 // g[k] -= sum_{i in [r0, r1)} L[i,k] g[i] for columns k in [k0, k0+kn), one warp per column.
+// Rows are read 16 bytes at a time between a scalar head and tail: a panel
+// column and the front vector start on 16-byte boundaries (panel offsets are
+// multiples of 64 elements, ldp and front-vector offsets of 8), so row i of
+// both is aligned exactly when i is a multiple of 16 / sizeof(element).
 template <class T, class Cv>
 __global__ void k_bwd_cols(const SolveBlockTask* __restrict__ tasks, SolveArgs A, const T* __restrict__ panel,
                            Cv* __restrict__ fv) {
+    static_assert(sizeof(T) == sizeof(Cv), "factor and vector elements of one size");
+    constexpr int V = 16 / (int)sizeof(T);
+    using Vec = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
     const SolveBlockTask tk = tasks[blockIdx.x];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (warp >= tk.kn) return;
     const SnDev d = A.sn[tk.s];
     const int k = tk.k0 + warp;
     const T* col = panel + d.panel_off + (long long)k * d.ldp;
+    const int head = min(tk.r1, (tk.r0 + V - 1) / V * V), body = max(head, tk.r1 / V * V);
     for (int r = 0; r < A.nrhs; ++r) {
         Cv* g = fv + A.fvec_off[tk.s] + r * A.fv_stride;
         Cv acc = Cv(0);
-        for (int i = tk.r0 + lane; i < tk.r1; i += 32) acc += (Cv)col[i] * g[i];
+        for (int i = tk.r0 + lane; i < head; i += 32) acc += (Cv)col[i] * g[i];
+        const Vec* cv = reinterpret_cast<const Vec*>(col);
+        const Vec* gv = reinterpret_cast<const Vec*>(g);
+        int v = head / V + lane;
+        for (; v + 32 < body / V; v += 64) {   // two 16-byte loads of each in flight per lane
+            const Vec a0 = cv[v], a1 = cv[v + 32], b0 = gv[v], b1 = gv[v + 32];
+            if constexpr (V == 4) {
+                acc += (Cv)a0.x * b0.x + (Cv)a0.y * b0.y + (Cv)a0.z * b0.z + (Cv)a0.w * b0.w;
+                acc += (Cv)a1.x * b1.x + (Cv)a1.y * b1.y + (Cv)a1.z * b1.z + (Cv)a1.w * b1.w;
+            } else {
+                acc += (Cv)a0.x * b0.x + (Cv)a0.y * b0.y;
+                acc += (Cv)a1.x * b1.x + (Cv)a1.y * b1.y;
+            }
+        }
+        for (; v < body / V; v += 32) {
+            const Vec a0 = cv[v], b0 = gv[v];
+            if constexpr (V == 4)
+                acc += (Cv)a0.x * b0.x + (Cv)a0.y * b0.y + (Cv)a0.z * b0.z + (Cv)a0.w * b0.w;
+            else
+                acc += (Cv)a0.x * b0.x + (Cv)a0.y * b0.y;
+        }
+        for (int i = body + lane; i < tk.r1; i += 32) acc += (Cv)col[i] * g[i];
         for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
         if (lane == 0) g[k] -= acc;
     }

@@ -147,7 +147,7 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
 // ---------------------------------------------------------------- kernel
 constexpr int kTcTile = 128;                  // M = N = 128
 constexpr int kTcBlockBytes = kTcTile * 128;  // one 128-row x 128-byte K block of one operand
-constexpr int kTcStages = 4;                  // shared-memory ring of (A, B) K blocks
+constexpr int kTcStages = 6;                  // shared-memory ring of (A, B) K blocks (192 KB: enough bytes in flight to cover load latency)
 constexpr int kTcGroup = 8;                   // column tiles per group of the tile order (L2 reuse)
 constexpr int kTcThreads = 192;               // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
 

@@ -269,3 +269,17 @@ def test_mixed_precision_multiple_rhs(gpu_lib):
     X = f.SolveRefined(B, tolerance=1e-10)
     for k in range(4):
         assert relative_residual(m, B[:, k], X[:, k]) <= 1e-10
+
+
+def test_symbolic_handle_destroyed_before_its_factor(gpu_lib):
+    """A garbage collector may finalise the symbolic object first: the factor stays usable."""
+    m = G.grid_matrix(6, 6, 6, 2)
+    b = build_vector(m.Size, 5)
+    s = SymmetricUtduSolver()
+    sym = s.Analyze(m)
+    f = s.Factorize(m, sym)
+    x0 = f.Solve(b)
+    sym.__del__()            # releases the native symbolic handle now
+    f.Refactorize(m)
+    assert np.array_equal(f.Solve(b), x0)
+    f.__del__()
