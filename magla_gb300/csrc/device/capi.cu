@@ -695,6 +695,8 @@ void run_solve(uchol_factor_s* F, int nrhs, Cv* work, Cv* fv, Cv* fv2, cudaStrea
         if (L.count == 0) continue;
         if (L.kind == SolveLaunch::FwdGather) {
             k_fwd_gather<Cv><<<L.count, 256, 0, st>>>(tasks + L.begin, A, work, fv);
+        } else if (L.kind == SolveLaunch::FwdSolo) {
+            k_fwd_solo<T, Cv, SB><<<L.count, 256, 0, st>>>(tasks + L.begin, A, panel, linv, fv, fv2, diag, work);
         } else {
             const int grid = F->coop_fwd;
             launch_cooperative(k_fwd_level<T, Cv, SB>, grid, 256, smem, st, level_args(L, fwd_flags, grid), A, panel,
@@ -707,6 +709,8 @@ void run_solve(uchol_factor_s* F, int nrhs, Cv* work, Cv* fv, Cv* fv2, cudaStrea
             k_bwd_gather<Cv><<<L.count, 256, 0, st>>>(tasks + L.begin, A, work, fv);
         } else if (L.kind == SolveLaunch::BwdTail) {
             k_bwd_cols<T, Cv><<<L.count, 256, 0, st>>>(tasks + L.begin, A, panel, fv);
+        } else if (L.kind == SolveLaunch::BwdSolo) {
+            k_bwd_solo<Cv, SB><<<L.count, 256, 0, st>>>(tasks + L.begin, A, linv, fv, fv2, work);
         } else {
             const int grid = F->coop_bwd;
             launch_cooperative(k_bwd_level<T, Cv, SB>, grid, 256, smem, st, level_args(L, bwd_flags, grid), A, panel,

@@ -487,11 +487,25 @@ Plan build_plan(int n, int count, const int* first_column, const int* parent, co
         P.progress_count += (int)bulk.size();
         return Lh;
     };
+    // fronts of one diagonal block go to the solo kernels, the others to the level kernels
+    auto split = [&](const std::vector<int>& fronts, std::vector<int>& multi) {
+        SolveLaunch S{SolveLaunch::FwdSolo, (int)P.solve_tasks.size(), 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+        multi.clear();
+        for (int s : fronts) {
+            if (P.sn[s].w <= SB) P.solve_tasks.push_back({s, 0, P.sn[s].w, 0, 0, 0, first_blk[s]});
+            else multi.push_back(s);
+        }
+        S.count = (int)P.solve_tasks.size() - S.begin;
+        return S;
+    };
+    std::vector<int> multi;
     for (int L = 0; L < P.levels; ++L) {
         const auto& fronts = at_level[L];
         auto g = gather_tasks(fronts);
         P.fwd_launches.push_back({SolveLaunch::FwdGather, g.first, g.second, 0, 0, 0, 0, 0, 0, 0, 0, 0});
-        P.fwd_launches.push_back(level_launch(SolveLaunch::FwdLevel, fronts, true));
+        SolveLaunch solo = split(fronts, multi);
+        if (solo.count > 0) P.fwd_launches.push_back(solo);
+        if (!multi.empty()) P.fwd_launches.push_back(level_launch(SolveLaunch::FwdLevel, multi, true));
     }
     for (int L = P.levels - 1; L >= 0; --L) {
         const auto& fronts = at_level[L];
@@ -505,7 +519,10 @@ Plan build_plan(int n, int count, const int* first_column, const int* parent, co
         }
         if ((int)P.solve_tasks.size() > tb)
             P.bwd_launches.push_back({SolveLaunch::BwdTail, tb, (int)P.solve_tasks.size() - tb, 0, 0, 0, 0, 0, 0, 0, 0, 0});
-        P.bwd_launches.push_back(level_launch(SolveLaunch::BwdLevel, fronts, false));
+        SolveLaunch solo = split(fronts, multi);
+        solo.kind = SolveLaunch::BwdSolo;
+        if (solo.count > 0) P.bwd_launches.push_back(solo);
+        if (!multi.empty()) P.bwd_launches.push_back(level_launch(SolveLaunch::BwdLevel, multi, false));
     }
     return P;
 }

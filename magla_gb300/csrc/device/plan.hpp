@@ -36,7 +36,7 @@ struct Launch {
 };
 
 struct SolveLaunch {
-    enum Kind : int { FwdGather, FwdLevel, BwdGather, BwdTail, BwdLevel } kind;
+    enum Kind : int { FwdGather, FwdSolo, FwdLevel, BwdGather, BwdTail, BwdSolo, BwdLevel } kind;
     int begin, count;   // tasks; level launches: the chains (one per front)
     int steps;          // level launches: most diagonal blocks of one front of the level
     int bulk_begin, bulk_count;   // level launches: the bulk chunks

@@ -551,17 +551,19 @@ __global__ void __launch_bounds__(256, 1) k_fwd_level(LevelArgs L, SolveArgs A, 
 template <class T, class Cv, int SB>
 __global__ void __launch_bounds__(256, 1) k_bwd_level(LevelArgs L, SolveArgs A, const T* __restrict__ panel,
                                                       const Cv* __restrict__ linv, Cv* fv, Cv* xv, Cv* work) {
-    constexpr int NP = SB / 32;   // column passes
     extern __shared__ __align__(128) unsigned char blk_smem[];
     unsigned char* sm = blk_smem + ((1024u - (smem_addr(blk_smem) & 1023u)) & 1023u);
     T* Tl = reinterpret_cast<T*>(sm);                          // tile L[b, b-1], column-major
     Cv* Li = reinterpret_cast<Cv*>(sm + SB * SB * sizeof(T));  // inverse of block b-1, column-major
     __shared__ Cv xb[SB];
     __shared__ Cv gb[SB];
+    __shared__ Cv part[256];
     __shared__ int ok;
     __shared__ unsigned long long tbar;
     __shared__ unsigned long long sbar[2];
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, nwarps = blockDim.x >> 5;
+    constexpr int TPC = 256 / SB;   // threads per column
+    constexpr int RPT = SB / TPC;   // rows per thread (a power of two)
+    const int tid = threadIdx.x, ccol = tid % SB, cpart = tid / SB;
     if ((int)blockIdx.x < L.nchain_cta) {
         // tile rows past a partial block are multiplied by zero: start from zeros, not stale bits
         for (int i = tid; i < SB * SB; i += blockDim.x) {
@@ -605,37 +607,55 @@ __global__ void __launch_bounds__(256, 1) k_bwd_level(LevelArgs L, SolveArgs A, 
                     __syncthreads();
                     for (int i = tid; i < SB; i += blockDim.x) xb[i] = i < kb ? __ldcg(xv + base + b * SB + i) : Cv(0);
                 }
+                // g of the block's columns, one load per thread (the bulk has finished with them)
+                for (int i = tid; i < kn; i += blockDim.x) gb[i] = __ldcg(fv + base + c0 + i);
                 if (r == 0) {
                     if (!__syncthreads_and(bar_wait(&tbar, phase, L.status))) return;
                     phase ^= 1;
                 }
                 __syncthreads();
-                // g_{b-1} -= L[b, b-1]^T x_b: warp per column of the tile (lanes over its rows)
-                for (int col = warp; col < kn; col += nwarps) {
-                    const Cv g0 = lane == 0 ? __ldcg(fv + base + c0 + col) : Cv(0);
+                // g_{b-1} -= L[b, b-1]^T x_b: thread (column, part) sums its part of the rows in
+                // skewed order (row part*RPT + (u + column) mod RPT), so that the threads of a warp
+                // read different banks of the column-major tile
+                if (t >= 0) {
                     Cv acc = Cv(0);
-                    if (t >= 0) {
-#pragma unroll
-                        for (int u = 0; u < SB / 32; ++u) acc += (Cv)Tl[lane + 32 * u + col * SB] * xb[lane + 32 * u];
-                        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+#pragma unroll 8
+                    for (int u = 0; u < RPT; ++u) {
+                        const int i = cpart * RPT + ((u + ccol) & (RPT - 1));
+                        acc += (Cv)Tl[i + ccol * SB] * xb[i];
                     }
-                    if (lane == 0) gb[col] = g0 - acc;
+                    part[tid] = acc;
                 }
                 __syncthreads();
-                // x = Li^T g: warp per output column of the inverse
-                for (int tt = warp; tt < kn; tt += nwarps) {
-                    Cv acc = Cv(0);
-                    for (int k = tt + lane; k < kn; k += 32) acc += Li[k + tt * SB] * gb[k];
-                    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-                    if (lane == 0) {
-                        xv[base + c0 + tt] = acc;
-                        xb[tt] = acc;   // x_{b-1}, kept for this front's next duty
-                        work[d.first_col + c0 + tt + (long long)r * A.ldw] = acc;
-                    }
+                if (t >= 0 && cpart == 0 && ccol < kn) {
+                    Cv sum = part[ccol];
+#pragma unroll
+                    for (int p = 1; p < TPC; ++p) sum += part[ccol + p * SB];
+                    gb[ccol] -= sum;
                 }
-                // a partial (last) block: the kept solution is zero past its width, as the tile
-                // rows it meets there hold whatever the copy left
-                for (int i = kn + tid; i < SB; i += blockDim.x) xb[i] = Cv(0);
+                __syncthreads();
+                // x = Li^T g: column tt of the inverse against g, the same skewed split (k >= tt)
+                {
+                    Cv acc = Cv(0);
+#pragma unroll 8
+                    for (int u = 0; u < RPT; ++u) {
+                        const int k = cpart * RPT + ((u + ccol) & (RPT - 1));
+                        if (k >= ccol && k < kn) acc += Li[k + ccol * SB] * gb[k];
+                    }
+                    part[tid] = acc;
+                }
+                __syncthreads();
+                if (cpart == 0) {
+                    Cv x = Cv(0);
+                    if (ccol < kn) {
+                        x = part[ccol];
+#pragma unroll
+                        for (int p = 1; p < TPC; ++p) x += part[ccol + p * SB];
+                        xv[base + c0 + ccol] = x;
+                        work[d.first_col + c0 + ccol + (long long)r * A.ldw] = x;
+                    }
+                    xb[ccol] = x;   // x_{b-1}, kept for this front's next duty (zero past a partial block)
+                }
             }
             held = q;
             publish(L.flags + c.blk + tgt, 1);
@@ -671,7 +691,7 @@ __global__ void __launch_bounds__(256, 1) k_bwd_level(LevelArgs L, SolveArgs A, 
             start_bulk_tile<T, SB>(stage(st_), L.maps + L.bulk[q].s, (L.bulk[q].k0 - t) * SB, L.bulk[q].r0, &sbar[st_]);
     };
     int seen_blk = -1, seen_b = -1, prev_q = -1;
-    Cv gcur[NP][4];
+    Cv gcur = Cv(0);   // g of this thread's column after the previous item (single right-hand side)
     int t0 = 0, q0 = -1;
     if (!next_item(t0, q0)) return;
     int t1 = t0, q1 = q0;
@@ -684,16 +704,10 @@ __global__ void __launch_bounds__(256, 1) k_bwd_level(LevelArgs L, SolveArgs A, 
         const SnDev d = A.sn[c.s];
         const int b = c.k0 - t0, kb = min(SB, d.w - b * SB);
         const bool same = c.blk == seen_blk && b == seen_b;
-        Cv gold[NP][4];
-        if (A.nrhs == 1 && lane == 0) {
-#pragma unroll
-            for (int p = 0; p < NP; ++p)
-#pragma unroll
-                for (int qq = 0; qq < 4; ++qq) {
-                    const int col = c.r0 + 4 * warp + 32 * p + qq;
-                    gold[p][qq] = col < c.r1 ? (q0 == prev_q ? gcur[p][qq] : fv[A.fvec_off[c.s] + col]) : Cv(0);
-                }
-        }
+        const int col = c.r0 + ccol;
+        // g of this thread's column, issued before the waits (this thread wrote it last, if anyone did)
+        Cv gold = Cv(0);
+        if (A.nrhs == 1 && cpart == 0 && col < c.r1) gold = q0 == prev_q ? gcur : fv[A.fvec_off[c.s] + col];
         if (!same && !wait_at_least(L.flags + c.blk + b, 1, L.status, &ok)) return;
         for (int r = 0; r < A.nrhs; ++r) {
             const long long base = A.fvec_off[c.s] + r * A.fv_stride;
@@ -708,21 +722,23 @@ __global__ void __launch_bounds__(256, 1) k_bwd_level(LevelArgs L, SolveArgs A, 
             }
             __syncthreads();
             const T* tile = stage(cur);
+            // thread (column, part): its part of the rows in skewed order (bank-conflict free)
+            Cv acc = Cv(0);
+#pragma unroll 8
+            for (int u = 0; u < RPT; ++u) {
+                const int i = cpart * RPT + ((u + ccol) & (RPT - 1));
+                acc += (Cv)tile[i + ccol * SB] * xb[i];
+            }
+            part[tid] = acc;
+            __syncthreads();
+            if (cpart == 0 && col < c.r1) {
+                Cv sum = part[ccol];
 #pragma unroll
-            for (int p = 0; p < NP; ++p)
-#pragma unroll
-                for (int qq = 0; qq < 4; ++qq) {
-                    const int cl = 4 * warp + 32 * p + qq, col = c.r0 + cl;
-                    Cv a = Cv(0);
-#pragma unroll
-                    for (int u = 0; u < SB / 32; ++u) a += (Cv)tile[lane + 32 * u + cl * SB] * xb[lane + 32 * u];
-                    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
-                    if (lane == 0 && col < c.r1) {
-                        const Cv gv = (A.nrhs == 1 ? gold[p][qq] : g[col]) - a;
-                        g[col] = gv;
-                        gcur[p][qq] = gv;
-                    }
-                }
+                for (int p = 1; p < TPC; ++p) sum += part[ccol + p * SB];
+                const Cv gv = (A.nrhs == 1 ? gold : g[col]) - sum;
+                g[col] = gv;
+                gcur = gv;
+            }
         }
         seen_blk = c.blk;
         seen_b = b;
@@ -739,6 +755,85 @@ __global__ void __launch_bounds__(256, 1) k_bwd_level(LevelArgs L, SolveArgs A, 
         q1 = q2;
         has1 = has2;
         cur ^= 1;
+    }
+}
+
+// Fronts of one diagonal block (most fronts low in the tree) need no chain:
+// one CTA per front solves its block and, forward, updates its trailing rows.
+
+// Forward: y = L_0^-1 f_0 (thread per row), y / D to the work vector, then
+// f[i] -= L[i, 0:w] y for the trailing rows (thread per row, coalesced columns).
+template <class T, class Cv, int SB>
+__global__ void __launch_bounds__(256) k_fwd_solo(const SolveBlockTask* __restrict__ tasks, SolveArgs A,
+                                                  const T* __restrict__ panel, const Cv* __restrict__ linv,
+                                                  Cv* __restrict__ fv, Cv* __restrict__ yv,
+                                                  const double* __restrict__ diag, Cv* __restrict__ work) {
+    __shared__ Cv f0[SB];
+    __shared__ Cv y[SB];
+    const SolveBlockTask tk = tasks[blockIdx.x];
+    const SnDev d = A.sn[tk.s];
+    const int w = d.w, tid = threadIdx.x;
+    const Cv* Li = linv + (long long)tk.blk * SB * SB;
+    const T* P = panel + d.panel_off;
+    for (int r = 0; r < A.nrhs; ++r) {
+        const long long base = A.fvec_off[tk.s] + r * A.fv_stride;
+        Cv* f = fv + base;
+        __syncthreads();
+        for (int t = tid; t < w; t += blockDim.x) f0[t] = f[t];
+        __syncthreads();
+        for (int t = tid; t < w; t += blockDim.x) {
+            Cv a0 = Cv(0), a1 = Cv(0);
+            int k = 0;
+            for (; k + 1 <= t; k += 2) {
+                a0 += Li[t + k * SB] * f0[k];
+                a1 += Li[t + (k + 1) * SB] * f0[k + 1];
+            }
+            for (; k <= t; ++k) a0 += Li[t + k * SB] * f0[k];
+            const Cv v = a0 + a1;
+            y[t] = v;
+            yv[base + t] = v;
+            work[d.first_col + t + (long long)r * A.ldw] = (Cv)((double)v / diag[d.first_col + t]);
+        }
+        __syncthreads();
+        for (int i = w + tid; i < d.m; i += blockDim.x) {
+            const T* row = P + i;
+            Cv a0 = Cv(0), a1 = Cv(0);
+            int k = 0;
+            for (; k + 1 < w; k += 2) {
+                a0 += (Cv)row[(long long)k * d.ldp] * y[k];
+                a1 += (Cv)row[(long long)(k + 1) * d.ldp] * y[k + 1];
+            }
+            for (; k < w; ++k) a0 += (Cv)row[(long long)k * d.ldp] * y[k];
+            f[i] -= a0 + a1;
+        }
+    }
+}
+
+// Backward: x = L_0^-T g (warp per output, lanes over the inverse's column),
+// after the trailing rows' contribution; x to the work vector.
+template <class Cv, int SB>
+__global__ void __launch_bounds__(256) k_bwd_solo(const SolveBlockTask* __restrict__ tasks, SolveArgs A,
+                                                  const Cv* __restrict__ linv, Cv* __restrict__ fv,
+                                                  Cv* __restrict__ xv, Cv* __restrict__ work) {
+    __shared__ Cv g0[SB];
+    const SolveBlockTask tk = tasks[blockIdx.x];
+    const SnDev d = A.sn[tk.s];
+    const int w = d.w, tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, nwarps = blockDim.x >> 5;
+    const Cv* Li = linv + (long long)tk.blk * SB * SB;
+    for (int r = 0; r < A.nrhs; ++r) {
+        const long long base = A.fvec_off[tk.s] + r * A.fv_stride;
+        __syncthreads();
+        for (int t = tid; t < w; t += blockDim.x) g0[t] = fv[base + t];
+        __syncthreads();
+        for (int t = warp; t < w; t += nwarps) {
+            Cv acc = Cv(0);
+            for (int k = t + lane; k < w; k += 32) acc += Li[k + t * SB] * g0[k];
+            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            if (lane == 0) {
+                xv[base + t] = acc;
+                work[d.first_col + t + (long long)r * A.ldw] = acc;
+            }
+        }
     }
 }
 
