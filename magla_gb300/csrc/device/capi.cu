@@ -8,6 +8,7 @@
 #include <climits>
 #include <cmath>
 #include <cstdlib>
+#include <cstdio>
 #include <cstring>
 #include <type_traits>
 #include <map>
@@ -355,13 +356,30 @@ void run_factor_launches(uchol_factor_s* F, cudaStream_t st) {
     if (timing) {
         CK(cudaStreamSynchronize(st));
         double sum[Launch::KindCount] = {0};
+        // optional per-launch record (diagnostics): kind, tasks, tiles, algorithmic tensor flops, largest K, ms
+        const char* log_path = getenv("UCHOL_LAUNCH_LOG");
+        FILE* log = log_path && *log_path ? fopen(log_path, "w") : nullptr;
+        if (log) fprintf(log, "kind,count,tiles,flops,max_k,ms\n");
         for (size_t q = 0; q < ev.size(); ++q) {
             float ms = 0.f;
             CK(cudaEventElapsedTime(&ms, ev[q].first, ev[q].second));
             sum[ev_kind[q]] += ms;
             cudaEventDestroy(ev[q].first);
             cudaEventDestroy(ev[q].second);
+            if (log) {
+                const Launch& L = P.launches[q];
+                double flops = 0.0;
+                int max_k = 0;
+                if (L.kind == Launch::TcUpdate)
+                    for (int j = L.begin; j < L.begin + L.count; ++j) {
+                        const TcJobHost& J = P.tc_jobs[j];
+                        flops += job_flops(UpdJob{0, J.s, J.c0, J.cend, J.kbeg, J.kn, -1}, P.sn[J.s]);
+                        max_k = std::max(max_k, J.kn);
+                    }
+                fprintf(log, "%d,%d,%lld,%.6e,%d,%.6f\n", (int)L.kind, L.count, L.tiles, flops, max_k, ms);
+            }
         }
+        if (log) fclose(log);
         F->phases.extend_add_ms = sum[Launch::ExtendAdd];
         F->phases.small_fronts_ms = sum[Launch::SmallFronts];
         F->phases.panel_ms = sum[Launch::PivotBlock] + sum[Launch::Trsm] + sum[Launch::DiagBlock] + sum[Launch::PanelSolve];

@@ -67,6 +67,8 @@ private:
     long long top_ = 0, peak_ = 0;
 };
 
+}  // namespace
+
 // Useful flops of an update job: 2 * kn per lower-triangle entry of columns [c0, cend), rows j..m-1.
 double job_flops(const UpdJob& J, const SnDev& d) {
     const double cols = J.cend - J.c0;
@@ -86,7 +88,6 @@ long long job_tiles(const UpdJob& J, const SnDev& d, int T) {
     return region(J.c0, J.cend);
 }
 
-}  // namespace
 
 Plan build_plan(int n, int count, const int* first_column, const int* parent, const int* child_ptr,
                 const int* children, const int* front_ptr, const int* front_rows, const int* diag_value_index,

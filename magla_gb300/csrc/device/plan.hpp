@@ -106,6 +106,10 @@ struct Plan {
     int progress_count = 0;                    // progress counters of all level launches
 };
 
+// Algorithmic flops (2 per multiply-add, lower triangle) and tiles of an update job.
+double job_flops(const UpdJob& J, const SnDev& d);
+long long job_tiles(const UpdJob& J, const SnDev& d, int T);
+
 // Throws std::runtime_error on inconsistent symbolic input.
 Plan build_plan(int n, int count, const int* first_column, const int* parent, const int* child_ptr,
                 const int* children, const int* front_ptr, const int* front_rows, const int* diag_value_index,
