@@ -165,7 +165,8 @@ int uchol_factor_phase_times(uchol_factor f, uchol_phase_times* t);
 
 /* Device memory a factorisation with these options will reserve, computed on
  * the host from the symbolic arrays alone (no GPU needed): factor panels,
- * the planned contribution arena and the tensor-core operand staging.
+ * the planned contribution arena and the tensor-core operand staging (with
+ * the K-split workspace of the tensor-core updates, 40 MB for a 152-SM GPU).
  * Counterpart of UtduSymbolicFactorization.EstimatePeakBytes
  * (CAESolvers/UCHOL/UtduSymbolicFactorization.cs:203-219). */
 int uchol_estimate_device_bytes(const uchol_symbolic_desc* desc, const uchol_options* opts, int64_t* factor_bytes,

@@ -199,6 +199,7 @@ struct uchol_factor_s {
     int factor_graph_nodes = 0;
     ~uchol_factor_s();
     DBuf maps;                    // tensor-map pairs of the staging regions
+    DBuf tc_ws, tc_counters;      // K-split tiles of the tensor-core updates: partial tiles, arrival counts
     int sms = 148;
     uchol_factor_stats last{};
     uchol_phase_times phases{};
@@ -339,10 +340,19 @@ void run_factor_launches(uchol_factor_s* F, cudaStream_t st) {
                 break;
             case Launch::KindCount:
                 throw Error(UCHOL_INTERNAL, "invalid launch kind");
-            case Launch::TcUpdate:
-                launch_tc_gemm(F->precision == UCHOL_PRECISION_BF16, D.tc_jobs.as<TcJob>() + L.begin, L.count, L.tiles,
-                               sn, (float*)panel, (float*)contrib, F->maps.as<CUtensorMap>(), &stats->status, F->sms, st);
+            case Launch::TcUpdate: {
+                // K blocks of every job when all share one K (the launch may then be split in K)
+                const bool bf16 = F->precision == UCHOL_PRECISION_BF16;
+                const int kbe = bf16 ? 64 : 32;
+                int nkb = (P.tc_jobs[L.begin].kn + kbe - 1) / kbe;
+                for (int j = L.begin + 1; j < L.begin + L.count; ++j)
+                    if (P.tc_jobs[j].kn != P.tc_jobs[L.begin].kn) nkb = 0;
+                const TcPlanned tp = tc_schedule(L.tiles, nkb, F->sms);
+                const TcSched S{L.tiles, tp.dp_tiles, tp.sk_nkb, F->tc_ws.as<float>(), F->tc_counters.as<int>()};
+                launch_tc_gemm(bf16, D.tc_jobs.as<TcJob>() + L.begin, L.count, S, tp.grid, sn, (float*)panel,
+                               (float*)contrib, F->maps.as<CUtensorMap>(), &stats->status, st);
                 break;
+            }
         }
         if (timing) CK(cudaEventRecord(ev.back().second, st));
         ++launches;
@@ -479,6 +489,8 @@ void enqueue_factorization(uchol_factor_s* F, cudaStream_t st) {
     if (S->full_nnz > 0) counted();
     if (S->count > 0) {
         CK(cudaMemsetAsync(F->panel.p, 0, F->panel.bytes, st));
+        // arrival counts of K-split tiles start at zero (also after a factorisation that timed out)
+        if (F->tc_counters.p) CK(cudaMemsetAsync(F->tc_counters.p, 0, F->tc_counters.bytes, st));
         if (F->elem == 8)
             k_assemble<double><<<grid_for(S->nnz, 256), 256, 0, st>>>(F->values.as<double>(), F->dp->asm_pos.as<long long>(),
                                                                       S->nnz, F->panel.as<double>());
@@ -593,18 +605,21 @@ uchol_factor_s* create_factor(uchol_symbolic_s* S, int n, int nnz, const uchol_o
         F->stage_b.alloc((size_t)P.stage_elems * op, "operand staging");
         CK(cudaMemsetAsync(F->stage_a.p, 0, F->stage_a.bytes, st));
         CK(cudaMemsetAsync(F->stage_b.p, 0, F->stage_b.bytes, st));
-        std::vector<CUtensorMap> maps;
-        maps.reserve(2 * P.map_front.size());
-        for (int s : P.map_front) {
+        std::vector<CUtensorMap> maps(2 * P.map_front.size());
+        for (size_t k = 0; k < P.map_front.size(); ++k) {
+            const int s = P.map_front[k];
             const StageInfo& g = P.stage[s];
             try {
-                maps.push_back(make_region_map(bf16, (char*)F->stage_a.p + g.off * op, P.sn[s].m, g.ld));
-                maps.push_back(make_region_map(bf16, (char*)F->stage_b.p + g.off * op, P.sn[s].m, g.ld));
+                make_stage_maps(bf16, (char*)F->stage_a.p + g.off * op, (char*)F->stage_b.p + g.off * op, P.sn[s].m,
+                                g.ld, &maps[2 * k]);
             } catch (const std::runtime_error& e) {
                 throw Error(UCHOL_CUDA_ERROR, e.what());
             }
         }
         F->maps.upload(maps, st, "tensor maps");
+        F->tc_ws.alloc(tc_ws_floats(F->sms) * sizeof(float), "K-split workspace");
+        F->tc_counters.alloc(tc_counter_count(F->sms) * sizeof(int), "K-split workspace");
+        CK(cudaMemsetAsync(F->tc_counters.p, 0, F->tc_counters.bytes, st));
         CK(cudaStreamSynchronize(st));
     }
     if (cfg.tensor_core)
@@ -1100,7 +1115,9 @@ int uchol_estimate_device_bytes(const uchol_symbolic_desc* d, const uchol_option
         if (factor_bytes) *factor_bytes = P.factor_elems * elem;
         if (contribution_bytes) *contribution_bytes = P.contrib_elems * elem;
         if (staging_bytes)
-            *staging_bytes = cfg.tensor_core ? 2 * P.stage_elems * op + (int64_t)P.diag_slots * kMinvStride * 4 : 0;
+            *staging_bytes = cfg.tensor_core ? 2 * P.stage_elems * op + (int64_t)P.diag_slots * kMinvStride * 4 +
+                                                   (int64_t)tc_ws_floats(152) * 4 + (int64_t)tc_counter_count(152) * 4
+                                             : 0;
         if (levels) *levels = P.levels;
         if (launches) *launches = (int)P.launches.size();
     });

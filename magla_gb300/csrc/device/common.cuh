@@ -92,6 +92,37 @@ __host__ __device__ __forceinline__ long long region_tiles(long long nc, long lo
     return nc * R - nc * (nc - 1) / 2;
 }
 
+// Tensor-core update tiles: 128 columns of C (the MMA's M side, TMEM lanes) by
+// 256 rows (its N side).  Column tile q of a job whose columns start h rows
+// above the front's end holds R_q = ceil((h - 128 q) / 256) row tiles, which
+// is R_0 - floor((q + delta) / 2) with delta = R_0 - R_1, so tile counts and
+// their prefixes have closed forms.
+constexpr int kTcCols = 128;
+constexpr int kTcRows = 256;
+
+// sum_{q < X} floor(q / 2)
+__host__ __device__ __forceinline__ long long tc_half_sum(long long X) {
+    const long long P = X >> 1;
+    return P * (P - 1) + ((X & 1) ? P : 0);
+}
+// R_0 and delta of a job with columns from c0 in a front of m rows.
+__host__ __device__ __forceinline__ void tc_col_shape(int c0, int m, int& R0, int& delta) {
+    const int h = m - c0;
+    R0 = (h + kTcRows - 1) / kTcRows;
+    delta = (h > kTcCols && (h - kTcCols + kTcRows - 1) / kTcRows < R0) ? 1 : 0;
+}
+// Tiles of the first Q column tiles.
+__host__ __device__ __forceinline__ long long tc_col_prefix(long long Q, int R0, int delta) {
+    return Q * R0 - tc_half_sum(Q + delta);
+}
+// Tiles of a whole update job: result columns [c0, cend) of a front with m rows.
+__host__ __device__ __forceinline__ long long tc_job_tiles(int c0, int cend, int m) {
+    if (cend <= c0) return 0;
+    int R0, delta;
+    tc_col_shape(c0, m, R0, delta);
+    return tc_col_prefix((cend - c0 + kTcCols - 1) / kTcCols, R0, delta);
+}
+
 #ifdef __CUDACC__
 // Decodes tile t of job J (front d) for tile edge T into (i0, j0, jend).
 __device__ __forceinline__ void decode_tile(const UpdJob& J, const SnDev& d, int T, long long t, int& i0, int& j0,

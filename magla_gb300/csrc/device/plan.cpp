@@ -299,19 +299,28 @@ Plan build_plan(int n, int count, const int* first_column, const int* parent, co
             }
             P.stage_elems = std::max(P.stage_elems, top);
         }
+        // tensor-core path, left-looking in two levels.  At the start of each super-block of
+        // kSuperBlocks outer blocks, one update brings all of its columns up to date with every
+        // earlier column of the supernode (K = sb0); each later outer block of the super-block
+        // then takes only the super-block's own earlier columns (K = k0 - sb0).  The operands
+        // W and L of K columns are read once per super-block instead of once per outer block:
+        // at 128-column blocks that update moves 2 bytes of W per 128 flops and is HBM-bound.
+        const int SBW = kSuperBlocks * NB;
         for (int k0 = 0; k0 < max_w; k0 += NB) {
-            // tensor-core path: left-looking update of the outer block [k0, k0+NB) with every
-            // earlier column of its supernode (K = k0), read once and written once
+            const int sb0 = k0 / SBW * SBW;
             if (cfg.tensor_core && k0 > 0) {
                 int jb = (int)P.tc_jobs.size();
                 long long tiles = 0;
                 for (int s : large) {
                     const SnDev& d = P.sn[s];
                     if (d.w <= k0) continue;
-                    int nbo = std::min(NB, d.w - k0);
-                    UpdJob U{tiles, s, k0, k0 + nbo, 0, k0, -1};
-                    P.tc_jobs.push_back({tiles, s, k0, k0 + nbo, 0, k0, P.stage[s].map});
-                    tiles += job_tiles(U, d, cfg.tc_tile_m);
+                    const bool super = k0 == sb0;
+                    const int cend = std::min(d.w, k0 + (super ? SBW : NB));
+                    const int kbeg = super ? 0 : sb0;
+                    const int kn = super ? k0 : k0 - sb0;
+                    UpdJob U{tiles, s, k0, cend, kbeg, kn, -1};
+                    P.tc_jobs.push_back({tiles, s, k0, cend, kbeg, kn, P.stage[s].map});
+                    tiles += tc_job_tiles(k0, cend, d.m);
                     P.tc_flops += job_flops(U, d);
                 }
                 if ((int)P.tc_jobs.size() > jb) P.launches.push_back({Launch::TcUpdate, jb, (int)P.tc_jobs.size() - jb, tiles});
@@ -404,7 +413,7 @@ Plan build_plan(int n, int count, const int* first_column, const int* parent, co
                 if (d.m == d.w) continue;
                 UpdJob U{tiles, s, d.w, d.m, 0, d.w, -1};
                 P.tc_jobs.push_back({tiles, s, d.w, d.m, 0, d.w, P.stage[s].map});
-                tiles += job_tiles(U, d, cfg.tc_tile_m);
+                tiles += tc_job_tiles(d.w, d.m, d.m);
                 P.tc_flops += job_flops(U, d);
             }
             if ((int)P.tc_jobs.size() > jb) P.launches.push_back({Launch::TcUpdate, jb, (int)P.tc_jobs.size() - jb, tiles});

@@ -13,14 +13,13 @@
 namespace uchol_dev {
 
 constexpr int kSolveRowsPlan = 128;   // rows per panel-solve task (kSolveRows of the kernel)
+constexpr int kSuperBlocks = 4;       // tensor-core path: outer blocks per super-block of the own-column updates
 
 struct PlanConfig {
     int pivot_block = 32;     // FP64 pivot block (the reference's PanelWidth)
     int outer_block = 32;     // Schur-update block (== pivot_block on the FP64 path)
     int small_max = 96;       // fronts with m <= small_max are factorised by one CTA in shared memory
     int tile = 64;            // SIMT tile edge (update kernels)
-    int tc_tile_m = 128;      // tensor-core tile
-    int tc_tile_n = 128;
     bool tensor_core = false; // outer updates on tcgen05 from staged operands
     int solve_block = 64;     // column block of the triangular solves
 };

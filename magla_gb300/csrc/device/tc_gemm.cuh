@@ -1,9 +1,20 @@
-// Tensor-core Schur update on sm_103a: C -= W L^T for 128 x 128 tiles of a
-// front's trailing lower triangle, with W = L21 D and L21 staged K-major in
-// low precision (FP32 read as TF32, or BF16).  Operands arrive through TMA
-// (128-byte swizzle) into shared memory, tcgen05.mma accumulates in TMEM
-// (FP32), and the epilogue subtracts the accumulator from the FP32 front in
-// place (column-major, one warp per 32 rows -> coalesced 128-byte columns).
+// Tensor-core Schur update on sm_103a: C -= W L^T over a front's trailing
+// lower triangle, with W = L21 D and L21 staged K-major in low precision (FP32
+// read as TF32, or BF16).  A tile is 128 columns x 256 rows of C computed
+// transposed, D = L_cols W_rows^T, by one M=128, N=256 tcgen05.mma per K step:
+// 48 KB of operands per 128-byte K block for 4.2 MFLOP (a 128 x 128 tile
+// moves 32 KB for half the flops), which is what bounds the kernel, since the
+// SM's operand bandwidth from L2 and HBM, not the tensor pipe, is the limit.
+// Operands arrive through TMA (128-byte swizzle) into a four-stage ring, the
+// accumulator lives in TMEM (two 256-column buffers), and eight epilogue warps
+// subtract it from the FP32 front in place: lane = column, so every thread
+// reads and writes 128 contiguous bytes of its column per 32-row chunk.
+//
+// Launches with few tiles are split in K (stream-K): the grid takes whole
+// tiles round robin while at least two waves remain, then divides the K
+// blocks of the remaining tiles evenly over all CTAs.  A CTA that ends with a
+// partial tile writes it to a workspace slot; the last of the tile's CTAs to
+// arrive adds the partial tiles in CTA order (deterministic) and updates C.
 //
 // Every wait on an mbarrier is bounded in time; on expiry the kernel records
 // a status word, waits once more (bounded) for its own operations, frees
@@ -145,46 +156,82 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
 }
 
 // ---------------------------------------------------------------- kernel
-constexpr int kTcTile = 128;                  // M = N = 128
-constexpr int kTcBlockBytes = kTcTile * 128;  // one 128-row x 128-byte K block of one operand
-constexpr int kTcStages = 6;                  // shared-memory ring of (A, B) K blocks (192 KB: enough bytes in flight to cover load latency)
-constexpr int kTcGroup = 8;                   // column tiles per group of the tile order (L2 reuse)
-constexpr int kTcThreads = 192;               // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
+constexpr int kTcABytes = kTcCols * 128;   // one 128-byte K block of the L operand (columns of C)
+constexpr int kTcBBytes = kTcRows * 128;   // one 128-byte K block of the W operand (rows of C)
+constexpr int kTcStages = 4;               // shared-memory ring of (A, B) K blocks: 192 KB
+constexpr int kTcGroup = 8;                // column tiles per group of the tile order (L2 reuse)
+constexpr int kTcEpiWarps = 8;             // two warps per TMEM lane quadrant, four 32-row chunks each
+constexpr int kTcThreads = 64 + 32 * kTcEpiWarps;   // warp 0 TMA, warp 1 MMA, warps 2-9 epilogue
+constexpr int kTcPartial = kTcCols * kTcRows;       // floats of one partial tile
+constexpr int kTcMinSplitKb = 8;           // K blocks of a tile below which it is never split
+constexpr int kTcMaxParts = 4;             // most CTAs sharing one split tile (bounds the fixup's reads)
 
 // One rank-kn update C[rows, cols] -= W[rows, kbeg:kbeg+kn] L[cols, kbeg:kbeg+kn]^T of front s,
-// operands in the front's staging region (tensor maps 2*map, 2*map+1; staging row = front row).
+// operands in the front's staging region (tensor maps 2*map (W, 256-row box), 2*map+1 (L,
+// 128-row box); staging row = front row).  Columns [c0, cend) lie all in the panel or all in
+// the contribution block.
 struct TcJob {
     long long tile_begin;
     int s, c0, cend, kbeg, kn, map;
 };
 
-// Tile t of a trapezoid of nc column tiles (first row tile count R), in
-// groups of G column tiles: inside a group, rows first, then the group's
-// columns, so the CTAs working at the same time share operand panels.
-__device__ __forceinline__ void decode_grouped(long long t, long long nc, long long R, int G, long long& jt,
-                                               long long& rt) {
-    for (long long jg = 0; jg < nc; jg += G) {
-        const long long g = min((long long)G, nc - jg);
-        const long long tri = g * (g + 1) / 2;
-        const long long count = tri + (R - jg - g) * g;
-        if (t < count) {
-            if (t < tri) {
-                long long dr = (long long)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
-                while (dr * (dr + 1) / 2 > t) --dr;
-                while ((dr + 1) * (dr + 2) / 2 <= t) ++dr;
-                rt = jg + dr;
-                jt = jg + (t - dr * (dr + 1) / 2);
-            } else {
-                const long long u = t - tri;
-                rt = jg + g + u / g;
-                jt = jg + u % g;
-            }
-            return;
-        }
-        t -= count;
+// Work split of one launch (see the file comment).
+struct TcSched {
+    long long tiles;      // tiles of the launch
+    long long dp_tiles;   // tiles [0, dp_tiles): whole tiles, round robin over the grid
+    int sk_nkb;           // > 0: tiles [dp_tiles, tiles) are split in K over the grid, sk_nkb K blocks each
+    float* ws;            // partial tiles: slots 2b and 2b + 1 of CTA b
+    int* counters;        // per split tile: partial tiles arrived (zero between launches)
+};
+
+// One unit of a CTA's work: K blocks [kb0, kb1) of tile t (kb1 < 0: all of the job's).
+struct TcSeg {
+    long long t;
+    int kb0, kb1;
+    int parts;   // 1: the whole tile; > 1: CTAs sharing the tile
+    int slot;    // workspace slot of a partial tile
+};
+
+// The segments of CTA b, in order; every role of the CTA walks the same sequence.
+struct TcSegIter {
+    long long t, dp, W, G, u, u0, u1;
+    int nkb, b;
+    __device__ TcSegIter(const TcSched& S, int b_, int G_) : t(b_), dp(S.dp_tiles), G(G_), nkb(S.sk_nkb), b(b_) {
+        W = nkb > 0 ? (S.tiles - dp) * nkb : 0;
+        u0 = u = W > 0 ? (long long)b * W / G : 0;
+        u1 = W > 0 ? (long long)(b + 1) * W / G : 0;
     }
-    jt = rt = 0;
-}
+    // CTA holding split unit v (units [b W / G, (b + 1) W / G) belong to CTA b)
+    __device__ long long owner(long long v) const { return ((v + 1) * G + W - 1) / W - 1; }
+    __device__ long long first_cta(long long tt) const { return owner(tt * nkb); }
+    __device__ long long last_cta(long long tt) const { return owner(tt * nkb + nkb - 1); }
+    // slot of CTA c's partial of split tile tt: its first segment uses 2c, its last 2c + 1
+    __device__ long long slot_of(long long c, long long tt) const { return c * W / G >= tt * nkb ? 2 * c : 2 * c + 1; }
+    __device__ bool next(TcSeg& g) {
+        if (t < dp) {
+            g.t = t;
+            g.kb0 = 0;
+            g.kb1 = -1;
+            g.parts = 1;
+            g.slot = 0;
+            t += G;
+            return true;
+        }
+        if (u < u1) {
+            const long long tt = u / nkb;
+            const int kb0 = (int)(u - tt * nkb);
+            const int kb1 = (int)min((long long)nkb, (long long)kb0 + (u1 - u));
+            g.t = dp + tt;
+            g.kb0 = kb0;
+            g.kb1 = kb1;
+            g.parts = (int)(last_cta(tt) - first_cta(tt) + 1);
+            g.slot = (int)(2 * b + (u == u0 ? 0 : 1));
+            u += kb1 - kb0;
+            return true;
+        }
+        return false;
+    }
+};
 
 __device__ __forceinline__ int tc_find_job(const TcJob* __restrict__ jobs, int njobs, long long t) {
     int lo = 0, hi = njobs - 1;
@@ -195,39 +242,116 @@ __device__ __forceinline__ int tc_find_job(const TcJob* __restrict__ jobs, int n
     return lo;
 }
 
-__device__ __forceinline__ void tc_tile(const TcJob& J, const SnDev& d, long long t, int& i0, int& j0, int& jend) {
-    int base = J.c0, lim = J.cend;
-    if (J.c0 < d.w && d.w < J.cend) {
-        const long long nc1 = (d.w - J.c0 + kTcTile - 1) / kTcTile;
-        const long long R1 = (d.m - J.c0 + kTcTile - 1) / kTcTile;
-        const long long n1 = region_tiles(nc1, R1);
-        if (t < n1) lim = d.w; else { t -= n1; base = d.w; }
+// Tile t of job J (front of m rows): first row i0, first column j0, column limit jend.
+// Column tiles go in groups of kTcGroup; inside a group, row tile r of every column
+// that has one, then r + 1, so the CTAs working at the same time share operand rows.
+__device__ __forceinline__ void tc_tile(const TcJob& J, int m, long long t, int& i0, int& j0, int& jend) {
+    const int nc = (J.cend - J.c0 + kTcCols - 1) / kTcCols;
+    int R0, delta;
+    tc_col_shape(J.c0, m, R0, delta);
+    int lo = 0, hi = (nc - 1) / kTcGroup;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (tc_col_prefix((long long)mid * kTcGroup, R0, delta) <= t) lo = mid; else hi = mid - 1;
     }
-    const long long nc = (lim - base + kTcTile - 1) / kTcTile;
-    const long long R = (d.m - base + kTcTile - 1) / kTcTile;
-    long long jt, rt;
-    decode_grouped(t, nc, R, kTcGroup, jt, rt);
-    j0 = base + (int)jt * kTcTile;
-    i0 = base + (int)rt * kTcTile;
-    jend = min(j0 + kTcTile, lim);
+    t -= tc_col_prefix((long long)lo * kTcGroup, R0, delta);
+    const int g = min(kTcGroup, nc - lo * kTcGroup);
+    const int Rg = R0 - lo * (kTcGroup / 2);
+    const int F = max(0, Rg - (g + delta + 1) / 2 + 1);   // rows every column of the group has
+    int r, q;
+    if (t < (long long)F * g) {
+        r = (int)(t / g);
+        q = (int)(t % g);
+    } else {
+        t -= (long long)F * g;
+        r = F;
+        q = 0;
+        for (int guard = 0; guard < kTcGroup; ++guard, ++r) {
+            const int c = min(g, max(0, 2 * (Rg - r) - delta));
+            if (t < c) {
+                q = (int)t;
+                break;
+            }
+            t -= c;
+        }
+    }
+    j0 = J.c0 + (lo * kTcGroup + q) * kTcCols;
+    i0 = j0 + r * kTcRows;
+    jend = min(j0 + kTcCols, J.cend);
+}
+
+// Barriers of the epilogue warps only (named barrier 1).  Every epilogue warp walks the
+// same segments and meets the same barriers; tc_epi_any also returns the OR of a
+// predicate over them, so that a decision to stop is the same in every warp.
+// Column j of C (indexed by front row) for the tile whose first column is j0.
+__device__ __forceinline__ float* tc_column(float* panel, float* contrib, const SnDev& d, int j0, int j) {
+    return j0 < d.w ? panel + d.panel_off + (long long)j * d.ldp
+                    : contrib + d.contrib_off + (long long)(j - d.w) * d.ldc - d.w;
+}
+
+__device__ __forceinline__ void tc_epi_sync() { asm volatile("bar.sync 1, %0;" ::"n"(32 * kTcEpiWarps) : "memory"); }
+__device__ __forceinline__ bool tc_epi_any(bool pred) {
+    uint32_t r;
+    asm volatile(
+        "{\n"
+        ".reg .pred p, q;\n"
+        "setp.ne.u32 p, %1, 0;\n"
+        "bar.red.or.pred q, 1, %2, p;\n"
+        "selp.u32 %0, 1, 0, q;\n"
+        "}\n"
+        : "=r"(r)
+        : "r"((uint32_t)pred), "n"(32 * kTcEpiWarps)
+        : "memory");
+    return r != 0;
+}
+
+// C[i0 + cc*32 + r, j] -= v[r] for the lower-triangle entries of rows below m; whole
+// float4 groups are read and written back (entries outside the triangle unchanged).
+__device__ __forceinline__ void tc_update_chunk(float* __restrict__ col, int ib, int j, int m, const float* v) {
+    float4 o[8];
+#pragma unroll
+    for (int r4 = 0; r4 < 8; ++r4) {
+        const int i = ib + 4 * r4;
+        if (i < m && i + 3 >= j) o[r4] = *reinterpret_cast<const float4*>(col + i);
+    }
+#pragma unroll
+    for (int r4 = 0; r4 < 8; ++r4) {
+        const int i = ib + 4 * r4;
+        if (i < m && i + 3 >= j) {
+            float4 x = o[r4];
+            if (i >= j && i + 3 < m) {
+                x.x -= v[4 * r4];
+                x.y -= v[4 * r4 + 1];
+                x.z -= v[4 * r4 + 2];
+                x.w -= v[4 * r4 + 3];
+            } else {
+                if (i >= j && i < m) x.x -= v[4 * r4];
+                if (i + 1 >= j && i + 1 < m) x.y -= v[4 * r4 + 1];
+                if (i + 2 >= j && i + 2 < m) x.z -= v[4 * r4 + 2];
+                if (i + 3 >= j && i + 3 < m) x.w -= v[4 * r4 + 3];
+            }
+            *reinterpret_cast<float4*>(col + i) = x;
+        }
+    }
 }
 
 template <bool BF16>
 __global__ void __launch_bounds__(kTcThreads, 1)
-    k_tc_gemm(const TcJob* __restrict__ jobs, int njobs, long long total_tiles, const SnDev* __restrict__ sn,
+    k_tc_gemm(const TcJob* __restrict__ jobs, int njobs, TcSched S, const SnDev* __restrict__ sn,
               float* __restrict__ panel, float* __restrict__ contrib, const CUtensorMap* __restrict__ maps,
               int* status) {
     constexpr int KBE = BF16 ? 64 : 32;  // K elements per 128-byte block
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    uint8_t* sA = smem;
-    uint8_t* sB = smem + kTcStages * kTcBlockBytes;
-    uint64_t* full = reinterpret_cast<uint64_t*>(sB + kTcStages * kTcBlockBytes);
+    uint8_t* sA = smem;                              // L rows (C columns)
+    uint8_t* sB = smem + kTcStages * kTcABytes;      // W rows (C rows)
+    uint64_t* full = reinterpret_cast<uint64_t*>(sB + kTcStages * kTcBBytes);
     uint64_t* empty = full + kTcStages;
     uint64_t* acc_full = empty + kTcStages;
     uint64_t* acc_empty = acc_full + 2;
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(acc_empty + 2);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+    volatile int* last_flag = reinterpret_cast<volatile int*>(tmem_slot + 2);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) {
@@ -237,13 +361,14 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         }
         for (int q = 0; q < 2; ++q) {
             mbar_init(&acc_full[q], 1);
-            mbar_init(&acc_empty[q], 128);
+            mbar_init(&acc_empty[q], 32 * kTcEpiWarps);
         }
         *abort_flag = 0;
+        *last_flag = 0;
         mbar_fence_init();
     }
     if (warp == 0) {
-        tmem_alloc(tmem_slot, 256);
+        tmem_alloc(tmem_slot, 2 * kTcRows);
         tmem_relinquish();
     }
     tc_fence_before();
@@ -261,22 +386,25 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         if (lane == 0) {
             int stage = 0;
             uint32_t phase = 0;
-            for (long long t = blockIdx.x; t < total_tiles && !*abort_flag; t += gridDim.x) {
-                const TcJob J = jobs[tc_find_job(jobs, njobs, t)];
-                const SnDev d = sn[J.s];
+            TcSegIter it(S, blockIdx.x, gridDim.x);
+            TcSeg g;
+            while (!*abort_flag && it.next(g)) {
+                const TcJob J = jobs[tc_find_job(jobs, njobs, g.t)];
                 int i0, j0, jend;
-                tc_tile(J, d, t - J.tile_begin, i0, j0, jend);
-                const CUtensorMap* ma = maps + 2 * J.map;
-                const CUtensorMap* mb = ma + 1;
-                const int nkb = (J.kn + KBE - 1) / KBE;
-                for (int kb = 0; kb < nkb; ++kb) {
-                    if (!mbar_wait(&empty[stage], phase ^ 1)) { fail(); break; }
-                    mbar_arrive_expect_tx(&full[stage], 2 * kTcBlockBytes);
+                tc_tile(J, sn[J.s].m, g.t - J.tile_begin, i0, j0, jend);
+                const CUtensorMap* mw = maps + 2 * J.map;
+                const CUtensorMap* ml = mw + 1;
+                const int kb1 = g.kb1 < 0 ? (J.kn + KBE - 1) / KBE : g.kb1;
+                bool ok = true;
+                for (int kb = g.kb0; kb < kb1; ++kb) {
+                    if (!mbar_wait(&empty[stage], phase ^ 1)) { fail(); ok = false; break; }
+                    mbar_arrive_expect_tx(&full[stage], kTcABytes + kTcBBytes);
                     const int kx = J.kbeg + kb * KBE;
-                    tma_load_2d(sA + stage * kTcBlockBytes, ma, &full[stage], kx, i0);
-                    tma_load_2d(sB + stage * kTcBlockBytes, mb, &full[stage], kx, j0);
+                    tma_load_2d(sA + stage * kTcABytes, ml, &full[stage], kx, j0);
+                    tma_load_2d(sB + stage * kTcBBytes, mw, &full[stage], kx, i0);
                     if (++stage == kTcStages) { stage = 0; phase ^= 1; }
                 }
+                if (!ok) break;
             }
         }
     } else if (warp == 1) {
@@ -286,22 +414,24 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             uint32_t phase = 0;
             int acc = 0;
             uint32_t acc_phase = 0;
-            constexpr uint32_t idesc = mma_idesc(BF16 ? 1u : 2u, kTcTile, kTcTile);
-            for (long long t = blockIdx.x; t < total_tiles && !*abort_flag; t += gridDim.x) {
-                const int nkb = (jobs[tc_find_job(jobs, njobs, t)].kn + KBE - 1) / KBE;
+            constexpr uint32_t idesc = mma_idesc(BF16 ? 1u : 2u, kTcCols, kTcRows);
+            TcSegIter it(S, blockIdx.x, gridDim.x);
+            TcSeg g;
+            while (!*abort_flag && it.next(g)) {
+                const int kb1 = g.kb1 < 0 ? (jobs[tc_find_job(jobs, njobs, g.t)].kn + KBE - 1) / KBE : g.kb1;
                 if (!mbar_wait(&acc_empty[acc], acc_phase ^ 1)) { fail(); break; }
                 tc_fence_after();
-                const uint32_t dt = tmem + (uint32_t)(acc * kTcTile);
+                const uint32_t dt = tmem + (uint32_t)(acc * kTcRows);
                 bool ok = true;
-                for (int kb = 0; kb < nkb; ++kb) {
+                for (int kb = g.kb0; kb < kb1; ++kb) {
                     if (!mbar_wait(&full[stage], phase)) { fail(); ok = false; break; }
                     tc_fence_after();
-                    const uint32_t a0 = smem_u32(sA + stage * kTcBlockBytes);
-                    const uint32_t b0 = smem_u32(sB + stage * kTcBlockBytes);
+                    const uint32_t a0 = smem_u32(sA + stage * kTcABytes);
+                    const uint32_t b0 = smem_u32(sB + stage * kTcBBytes);
 #pragma unroll
                     for (int kk = 0; kk < 4; ++kk)
                         umma<BF16>(dt, sw128_desc(a0 + kk * 32), sw128_desc(b0 + kk * 32), idesc,
-                                   (kb | kk) != 0 ? 1u : 0u);
+                                   (kb != g.kb0 || kk != 0) ? 1u : 0u);
                     umma_commit(&empty[stage]);
                     if (++stage == kTcStages) { stage = 0; phase ^= 1; }
                 }
@@ -311,43 +441,113 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             }
         }
     } else {
-        // ---------------- epilogue: warps 2..5 own TMEM lanes 32*(warp%4) .. +31
+        // ---------------- epilogue: warp w reads TMEM lanes 32*(w%4) .. +31 (columns of C)
+        // and 32-row chunks [4h, 4h + 4), h = (w - 2) / 4
         const int q = warp & 3;
+        const int c_first = ((warp - 2) >> 2) * 4;
+        const int jl = q * 32 + lane;
         int acc = 0;
         uint32_t acc_phase = 0;
-        for (long long t = blockIdx.x; t < total_tiles; t += gridDim.x) {
-            const TcJob J = jobs[tc_find_job(jobs, njobs, t)];
+        TcSegIter it(S, blockIdx.x, gridDim.x);
+        TcSeg g;
+        for (;;) {
+            const bool have = it.next(g);
+            if (tc_epi_any(!have || *abort_flag)) break;
+            const TcJob J = jobs[tc_find_job(jobs, njobs, g.t)];
             const SnDev d = sn[J.s];
             int i0, j0, jend;
-            tc_tile(J, d, t - J.tile_begin, i0, j0, jend);
-            if (!mbar_wait(&acc_full[acc], acc_phase)) { fail(); break; }
+            tc_tile(J, d.m, g.t - J.tile_begin, i0, j0, jend);
+            // on an expired wait this thread skips its work but still meets the barriers below
+            const bool ok = __all_sync(0xffffffffu, mbar_wait(&acc_full[acc], acc_phase));   // warp-uniform
+            if (!ok) fail();
             tc_fence_after();
-            const int i = i0 + q * 32 + lane;
-            const bool in_panel = j0 < d.w;
-            float* base = in_panel ? panel + d.panel_off + i : contrib + d.contrib_off + (i - d.w);
-            const long long ldc = in_panel ? d.ldp : d.ldc;
-            const int jshift = in_panel ? 0 : d.w;
-            const bool row_ok = i < d.m;
-            const uint32_t ta = tmem + (uint32_t)(acc * kTcTile) + ((uint32_t)(q * 32) << 16);
+            const int j = j0 + jl;
+            float* col = tc_column(panel, contrib, d, j0, j);   // column j of C, indexed by front row
+            const uint32_t ta = tmem + (uint32_t)(acc * kTcRows) + ((uint32_t)(q * 32) << 16);
+            if (g.parts == 1) {
+                if (ok) {
 #pragma unroll 1
-            for (int cc = 0; cc < kTcTile / 32; ++cc) {
-                float v[32], old[32];
-                tmem_ld32(ta + (uint32_t)(cc * 32), v);
-#pragma unroll
-                for (int c = 0; c < 32; ++c) {
-                    const int j = j0 + cc * 32 + c;
-                    old[c] = (row_ok && j < jend && i >= j) ? base[(long long)(j - jshift) * ldc] : 0.f;
+                    for (int cc = c_first; cc < c_first + 4; ++cc) {
+                        float v[32];
+                        tmem_ld32(ta + (uint32_t)(cc * 32), v);
+                        if (j < jend) tc_update_chunk(col, i0 + cc * 32, j, d.m, v);
+                    }
                 }
+            } else {
+                // partial tile: to the workspace; the last CTA of the tile adds all of them
+                if (ok) {
+                    float* mine = S.ws + (long long)g.slot * kTcPartial + (long long)jl * kTcRows;
+#pragma unroll 1
+                    for (int cc = c_first; cc < c_first + 4; ++cc) {
+                        float v[32];
+                        tmem_ld32(ta + (uint32_t)(cc * 32), v);
 #pragma unroll
-                for (int c = 0; c < 32; ++c) {
-                    const int j = j0 + cc * 32 + c;
-                    if (row_ok && j < jend && i >= j) base[(long long)(j - jshift) * ldc] = old[c] - v[c];
+                        for (int r4 = 0; r4 < 8; ++r4)
+                            __stcg(reinterpret_cast<float4*>(mine + cc * 32) + r4,
+                                   make_float4(v[4 * r4], v[4 * r4 + 1], v[4 * r4 + 2], v[4 * r4 + 3]));
+                    }
+                }
+                __threadfence();
+                const bool bad = tc_epi_any(!ok);
+                const long long tt = g.t - it.dp;
+                if (threadIdx.x == 64) {
+                    int last = 0;
+                    if (!bad) {
+                        const int before = atomicAdd(&S.counters[tt], 1);
+                        last = before == g.parts - 1;
+                        if (last) S.counters[tt] = 0;
+                    }
+                    *last_flag = last;
+                    __threadfence();
+                }
+                tc_epi_sync();
+                if (*last_flag) {
+                    __threadfence();
+                    const long long c_lo = it.first_cta(tt), c_hi = it.last_cta(tt);
+#pragma unroll 1
+                    for (int cc = c_first; cc < c_first + 4; ++cc) {
+                        float v[32];
+#pragma unroll
+                        for (int r = 0; r < 32; ++r) v[r] = 0.f;
+                        // two partial tiles in flight per step, added in CTA order
+#pragma unroll 1
+                        for (long long c = c_lo; c <= c_hi; c += 2) {
+                            const float4* p0 = reinterpret_cast<const float4*>(
+                                S.ws + it.slot_of(c, tt) * kTcPartial + (long long)jl * kTcRows + cc * 32);
+                            const bool two = c + 1 <= c_hi;
+                            const float4* p1 = reinterpret_cast<const float4*>(
+                                S.ws + it.slot_of(two ? c + 1 : c, tt) * kTcPartial + (long long)jl * kTcRows + cc * 32);
+                            float4 x0[8], x1[8];
+#pragma unroll
+                            for (int r4 = 0; r4 < 8; ++r4) {
+                                x0[r4] = __ldcg(p0 + r4);
+                                if (two) x1[r4] = __ldcg(p1 + r4);
+                            }
+#pragma unroll
+                            for (int r4 = 0; r4 < 8; ++r4) {
+                                v[4 * r4] += x0[r4].x;
+                                v[4 * r4 + 1] += x0[r4].y;
+                                v[4 * r4 + 2] += x0[r4].z;
+                                v[4 * r4 + 3] += x0[r4].w;
+                            }
+                            if (two) {
+#pragma unroll
+                                for (int r4 = 0; r4 < 8; ++r4) {
+                                    v[4 * r4] += x1[r4].x;
+                                    v[4 * r4 + 1] += x1[r4].y;
+                                    v[4 * r4 + 2] += x1[r4].z;
+                                    v[4 * r4 + 3] += x1[r4].w;
+                                }
+                            }
+                        }
+                        if (j < jend) tc_update_chunk(col, i0 + cc * 32, j, d.m, v);
+                    }
                 }
             }
+            // the accumulator is free once every thread has read it (for a partial tile: written it out)
             tc_fence_before();
             mbar_arrive(&acc_empty[acc]);
             if (++acc == 2) { acc = 0; acc_phase ^= 1; }
-            if (*abort_flag) break;
         }
     }
     tc_fence_before();
@@ -359,7 +559,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         }
     }
     __syncthreads();
-    if (warp == 0) tmem_dealloc(tmem, 256);
+    if (warp == 0) tmem_dealloc(tmem, 2 * kTcRows);
 }
 
 // ---------------------------------------------------------------- host side
@@ -376,14 +576,14 @@ inline PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
     return fn;
 }
 
-// A K-major [rows x ld] operand region: box = 128 bytes of K x 128 rows,
+// A K-major [rows x ld] operand region: box = 128 bytes of K x box_rows rows,
 // 128-byte swizzle, zero fill outside (rows beyond the front, K beyond ld).
-inline CUtensorMap make_region_map(bool bf16, void* base, long long rows, int ld) {
+inline CUtensorMap make_region_map(bool bf16, void* base, long long rows, int ld, int box_rows) {
     CUtensorMap m;
     const size_t es = bf16 ? 2 : 4;
     cuuint64_t dims[2] = {(cuuint64_t)ld, (cuuint64_t)rows};
     cuuint64_t strides[1] = {(cuuint64_t)ld * es};
-    cuuint32_t box[2] = {(cuuint32_t)(128 / es), (cuuint32_t)kTcTile};
+    cuuint32_t box[2] = {(cuuint32_t)(128 / es), (cuuint32_t)box_rows};
     cuuint32_t estr[2] = {1, 1};
     CUresult r = tensor_map_encoder()(&m, bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
                                       base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
@@ -393,18 +593,53 @@ inline CUtensorMap make_region_map(bool bf16, void* base, long long rows, int ld
     return m;
 }
 
-inline size_t tc_smem_bytes() {
-    return (size_t)kTcStages * 2 * kTcBlockBytes + 1024 + (2 * kTcStages + 4) * 8 + 16;
+// The tensor-map pair of one front's staging regions: W rows (256-row box), L rows (128-row box).
+inline void make_stage_maps(bool bf16, void* w_base, void* l_base, long long rows, int ld, CUtensorMap* out) {
+    out[0] = make_region_map(bf16, w_base, rows, ld, kTcRows);
+    out[1] = make_region_map(bf16, l_base, rows, ld, kTcCols);
 }
 
-inline void launch_tc_gemm(bool bf16, const TcJob* jobs, int njobs, long long tiles, const SnDev* sn, float* panel,
-                           float* contrib, const CUtensorMap* maps, int* status, int sms, cudaStream_t st) {
+inline size_t tc_smem_bytes() {
+    return (size_t)kTcStages * (kTcABytes + kTcBBytes) + 1024 + (2 * kTcStages + 4) * 8 + 16;
+}
+
+// Workspace of the K-split tiles: two partial tiles per CTA, one counter per split tile.
+inline size_t tc_ws_floats(int sms) { return (size_t)2 * sms * kTcPartial; }
+inline size_t tc_counter_count(int sms) { return (size_t)2 * sms; }
+
+// Grid and split of one launch of `tiles` tiles.  nkb: K blocks of every tile when all
+// tiles have the same K (0 otherwise: never split).  Time is counted in K blocks per CTA;
+// a split tile costs about kTcMinSplitKb more (its partial tiles through L2).
+struct TcPlanned {
+    unsigned grid;
+    long long dp_tiles;
+    int sk_nkb;
+};
+inline TcPlanned tc_schedule(long long tiles, int nkb, int sms) {
+    TcPlanned p{(unsigned)std::max<long long>(1, std::min<long long>(tiles, sms)), tiles, 0};
+    if (nkb < kTcMinSplitKb || tiles <= 0) return p;
+    const long long waves = (tiles + sms - 1) / sms;
+    const double t_dp = (double)waves * nkb;
+    long long G = sms;
+    const long long dp = tiles >= 2LL * G ? (tiles / G - 1) * G : 0;
+    const long long W = (tiles - dp) * nkb;
+    if (dp == 0) G = std::max<long long>(1, std::min<long long>({G, W / kTcMinSplitKb, tiles * kTcMaxParts}));
+    const double t_sk = (double)(dp / G) * nkb + (double)((W + G - 1) / G) + kTcMinSplitKb;
+    if (t_sk < 0.9 * t_dp) {
+        p.grid = (unsigned)G;
+        p.dp_tiles = dp;
+        p.sk_nkb = nkb;
+    }
+    return p;
+}
+
+inline void launch_tc_gemm(bool bf16, const TcJob* jobs, int njobs, const TcSched& S, unsigned grid, const SnDev* sn,
+                           float* panel, float* contrib, const CUtensorMap* maps, int* status, cudaStream_t st) {
     const size_t smem = tc_smem_bytes();
-    const unsigned grid = (unsigned)std::min<long long>(tiles, (long long)sms);
     if (bf16) {
-        k_tc_gemm<true><<<grid, kTcThreads, smem, st>>>(jobs, njobs, tiles, sn, panel, contrib, maps, status);
+        k_tc_gemm<true><<<grid, kTcThreads, smem, st>>>(jobs, njobs, S, sn, panel, contrib, maps, status);
     } else {
-        k_tc_gemm<false><<<grid, kTcThreads, smem, st>>>(jobs, njobs, tiles, sn, panel, contrib, maps, status);
+        k_tc_gemm<false><<<grid, kTcThreads, smem, st>>>(jobs, njobs, S, sn, panel, contrib, maps, status);
     }
 }
 
