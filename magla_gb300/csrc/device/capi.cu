@@ -730,6 +730,8 @@ void run_solve(uchol_factor_s* F, int nrhs, Cv* work, Cv* fv, Cv* fv2, cudaStrea
             k_fwd_gather<Cv><<<L.count, 256, 0, st>>>(tasks + L.begin, A, work, fv);
         } else if (L.kind == SolveLaunch::FwdSolo) {
             k_fwd_solo<T, Cv, SB><<<L.count, 256, 0, st>>>(tasks + L.begin, A, panel, linv, fv, fv2, diag, work);
+        } else if (L.kind == SolveLaunch::FwdTail) {
+            k_fwd_tail<T, Cv, SB><<<L.count, kTailRows / 4, 0, st>>>(tasks + L.begin, A, panel, fv2, fv);
         } else {
             const int grid = F->coop_fwd;
             launch_cooperative(k_fwd_level<T, Cv, SB>, grid, 256, smem, st, level_args(L, fwd_flags, grid), A, panel,
@@ -752,6 +754,8 @@ void run_solve(uchol_factor_s* F, int nrhs, Cv* work, Cv* fv, Cv* fv2, cudaStrea
     }
     CK(cudaGetLastError());
 }
+
+static_assert(kTailRows == kTailRowsPlan, "forward tail chunk of the plan and the kernel");
 
 int solve_launch_count(const Plan& P) {
     int c = 0;

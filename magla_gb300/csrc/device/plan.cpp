@@ -515,6 +515,16 @@ Plan build_plan(int n, int count, const int* first_column, const int* parent, co
         P.fwd_launches.push_back({SolveLaunch::FwdGather, g.first, g.second, 0, 0, 0, 0, 0, 0, 0, 0, 0});
         SolveLaunch solo = split(fronts, multi);
         if (solo.count > 0) P.fwd_launches.push_back(solo);
+        // trailing rows of the single-block fronts, in chunks from w rounded down to 4
+        int tb = (int)P.solve_tasks.size();
+        for (int s : fronts) {
+            const SnDev& d = P.sn[s];
+            if (d.w > SB || d.m == d.w) continue;
+            for (int r = d.w & ~3; r < d.m; r += kTailRowsPlan)
+                P.solve_tasks.push_back({s, 0, d.w, r, std::min(d.m, r + kTailRowsPlan), 0, 0});
+        }
+        if ((int)P.solve_tasks.size() > tb)
+            P.fwd_launches.push_back({SolveLaunch::FwdTail, tb, (int)P.solve_tasks.size() - tb, 0, 0, 0, 0, 0, 0, 0, 0, 0});
         if (!multi.empty()) P.fwd_launches.push_back(level_launch(SolveLaunch::FwdLevel, multi, true));
     }
     for (int L = P.levels - 1; L >= 0; --L) {

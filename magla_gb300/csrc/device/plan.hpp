@@ -13,6 +13,7 @@
 namespace uchol_dev {
 
 constexpr int kSolveRowsPlan = 128;   // rows per panel-solve task (kSolveRows of the kernel)
+constexpr int kTailRowsPlan = 1024;  // trailing rows per forward tail task (kTailRows of the kernel)
 constexpr int kSuperBlocks = 4;       // tensor-core path: outer blocks per super-block of the own-column updates
 
 struct PlanConfig {
@@ -35,7 +36,7 @@ struct Launch {
 };
 
 struct SolveLaunch {
-    enum Kind : int { FwdGather, FwdSolo, FwdLevel, BwdGather, BwdTail, BwdSolo, BwdLevel } kind;
+    enum Kind : int { FwdGather, FwdSolo, FwdLevel, BwdGather, BwdTail, BwdSolo, BwdLevel, FwdTail } kind;
     int begin, count;   // tasks; level launches: the chains (one per front)
     int steps;          // level launches: most diagonal blocks of one front of the level
     int bulk_begin, bulk_count;   // level launches: the bulk chunks

@@ -794,18 +794,70 @@ __global__ void __launch_bounds__(256) k_fwd_solo(const SolveBlockTask* __restri
             yv[base + t] = v;
             work[d.first_col + t + (long long)r * A.ldw] = (Cv)((double)v / diag[d.first_col + t]);
         }
+    }
+}
+
+// Four consecutive entries of a factor column (16- or 32-byte aligned), widened.
+__device__ __forceinline__ void load4(const float* p, float* v) {
+    const float4 x = *reinterpret_cast<const float4*>(p);
+    v[0] = x.x;
+    v[1] = x.y;
+    v[2] = x.z;
+    v[3] = x.w;
+}
+__device__ __forceinline__ void load4(const double* p, double* v) {
+    const double2 x = reinterpret_cast<const double2*>(p)[0], z = reinterpret_cast<const double2*>(p)[1];
+    v[0] = x.x;
+    v[1] = x.y;
+    v[2] = z.x;
+    v[3] = z.y;
+}
+
+// Forward, trailing rows of single-block fronts (after k_fwd_solo): f[i] -= sum_k L[i, k] y[k]
+// for rows [r0, r1) of the task's front (r0 a multiple of 4; rows below w are skipped).
+// Four consecutive rows per thread, one aligned group per column, eight columns in flight,
+// so a front's trailing block streams at HBM speed over many CTAs instead of one.
+constexpr int kTailRows = 1024;
+template <class T, class Cv, int SB>
+__global__ void __launch_bounds__(kTailRows / 4) k_fwd_tail(const SolveBlockTask* __restrict__ tasks, SolveArgs A,
+                                                            const T* __restrict__ panel, const Cv* __restrict__ yv,
+                                                            Cv* __restrict__ fv) {
+    __shared__ Cv y[SB];
+    const SolveBlockTask tk = tasks[blockIdx.x];
+    const SnDev d = A.sn[tk.s];
+    const int w = d.w;
+    const int i = tk.r0 + 4 * (int)threadIdx.x;
+    const T* p = panel + d.panel_off + i;
+    for (int r = 0; r < A.nrhs; ++r) {
+        const long long base = A.fvec_off[tk.s] + r * A.fv_stride;
         __syncthreads();
-        for (int i = w + tid; i < d.m; i += blockDim.x) {
-            const T* row = P + i;
-            Cv a0 = Cv(0), a1 = Cv(0);
-            int k = 0;
-            for (; k + 1 < w; k += 2) {
-                a0 += (Cv)row[(long long)k * d.ldp] * y[k];
-                a1 += (Cv)row[(long long)(k + 1) * d.ldp] * y[k + 1];
+        for (int t = threadIdx.x; t < w; t += blockDim.x) y[t] = __ldcg(yv + base + t);
+        __syncthreads();
+        if (i >= tk.r1) continue;
+        Cv a[4] = {Cv(0), Cv(0), Cv(0), Cv(0)};
+        int k = 0;
+        for (; k + 8 <= w; k += 8) {
+            T v[8][4];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) load4(p + (long long)(k + u) * d.ldp, v[u]);
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const Cv yk = y[k + u];
+#pragma unroll
+                for (int e = 0; e < 4; ++e) a[e] += (Cv)v[u][e] * yk;
             }
-            for (; k < w; ++k) a0 += (Cv)row[(long long)k * d.ldp] * y[k];
-            f[i] -= a0 + a1;
         }
+        for (; k < w; ++k) {
+            T v[4];
+            load4(p + (long long)k * d.ldp, v);
+            const Cv yk = y[k];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) a[e] += (Cv)v[e] * yk;
+        }
+        Cv* f = fv + base;
+#pragma unroll
+        for (int e = 0; e < 4; ++e)
+            if (i + e >= w && i + e < tk.r1) f[i + e] -= a[e];
     }
 }
 
