@@ -253,9 +253,10 @@ __device__ __forceinline__ bool wait_at_least(const int* flag, int target, int* 
     return r;
 }
 
-// Every thread's writes, then the flag (release).
+// Every thread's writes, then the flag: the CTA barrier orders the other threads' writes
+// before thread 0's release store, and release is cumulative, so a reader that acquires the
+// flag (ld.acquire.gpu, then a CTA barrier) sees all of them.
 __device__ __forceinline__ void publish(int* flag, int value) {
-    __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) st_release_gpu(flag, value);
 }
@@ -387,11 +388,8 @@ __global__ void __launch_bounds__(256, 1) k_fwd_level(LevelArgs L, SolveArgs A, 
         for (;;) {
             front(q);
             const int r0 = (b + 1) * SB, kn = min(SB, d.w - r0);
-            // the bulk chunk of block b+1 has applied y_0 .. y_{b-1}
-            if (b >= 1 && !wait_at_least(L.progress + c.k0 + b + 1, b, L.status, &ok)) return;
             for (int r = 0; r < A.nrhs; ++r) {
                 const long long base = A.fvec_off[c.s] + r * A.fv_stride;
-                const Cv f0 = (pid == 0 && row < kn) ? __ldcg(fv + base + r0 + row) : Cv(0);
                 if (b >= 0 && !(A.nrhs == 1 && held == q)) {
                     __syncthreads();
                     for (int t = tid; t < SB; t += blockDim.x) yb[t] = __ldcg(yv + base + b * SB + t);
@@ -408,6 +406,10 @@ __global__ void __launch_bounds__(256, 1) k_fwd_level(LevelArgs L, SolveArgs A, 
                     for (int u = 0; u < CPT; ++u) a4[u & 3] += (Cv)Tl[row + (pid * CPT + u) * SB] * yb[pid * CPT + u];
                 }
                 part[tid] = (a4[0] + a4[1]) + (a4[2] + a4[3]);
+                // only now the bulk's part: chunk b+1 has applied y_0 .. y_{b-1} (the product above
+                // needs neither it nor f, so it overlaps the bulk's last update)
+                if (r == 0 && b >= 1 && !wait_at_least(L.progress + c.k0 + b + 1, b, L.status, &ok)) return;
+                const Cv f0 = (pid == 0 && row < kn) ? __ldcg(fv + base + r0 + row) : Cv(0);
                 __syncthreads();
                 if (pid == 0) {
                     Cv v = f0;
@@ -599,16 +601,12 @@ __global__ void __launch_bounds__(256, 1) k_bwd_level(LevelArgs L, SolveArgs A, 
             const int tgt = b - 1;                             // block solved by this duty
             const int c0 = tgt * SB, kn = min(SB, d.w - c0);
             const int kb = t >= 0 ? min(SB, d.w - b * SB) : 0;  // rows of block b
-            // the bulk chunk of block b-1 has applied x_{nblk-1} .. x_{b+1}
-            if (t >= 1 && !wait_at_least(L.progress + c.k0 + tgt, t, L.status, &ok)) return;
             for (int r = 0; r < A.nrhs; ++r) {
                 const long long base = A.fvec_off[c.s] + r * A.fv_stride;
                 if (t >= 0 && !(A.nrhs == 1 && held == q)) {
                     __syncthreads();
                     for (int i = tid; i < SB; i += blockDim.x) xb[i] = i < kb ? __ldcg(xv + base + b * SB + i) : Cv(0);
                 }
-                // g of the block's columns, one load per thread (the bulk has finished with them)
-                for (int i = tid; i < kn; i += blockDim.x) gb[i] = __ldcg(fv + base + c0 + i);
                 if (r == 0) {
                     if (!__syncthreads_and(bar_wait(&tbar, phase, L.status))) return;
                     phase ^= 1;
@@ -626,6 +624,10 @@ __global__ void __launch_bounds__(256, 1) k_bwd_level(LevelArgs L, SolveArgs A, 
                     }
                     part[tid] = acc;
                 }
+                // only now the bulk's part: chunk b-1 has applied x_{nblk-1} .. x_{b+1}; then g of
+                // the block's columns, one load per thread
+                if (r == 0 && t >= 1 && !wait_at_least(L.progress + c.k0 + tgt, t, L.status, &ok)) return;
+                for (int i = tid; i < kn; i += blockDim.x) gb[i] = __ldcg(fv + base + c0 + i);
                 __syncthreads();
                 if (t >= 0 && cpart == 0 && ccol < kn) {
                     Cv sum = part[ccol];
