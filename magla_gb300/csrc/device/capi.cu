@@ -327,11 +327,11 @@ void run_factor_launches(uchol_factor_s* F, cudaStream_t st) {
                         k_diag_block<<<L.count, 256, kDiagSmemBytes, st>>>(D.pivot_tasks.as<PanelTask>() + L.begin, sn,
                                                                            panel, diag, F->minv.as<float>(), ctl, stats);
                     else if (F->precision == UCHOL_PRECISION_BF16)
-                        k_panel_solve<__nv_bfloat16><<<L.count, 256, 0, st>>>(
+                        k_panel_solve<__nv_bfloat16><<<L.count, 256, kPanelSmemBytes, st>>>(
                             D.panel_tasks.as<PanelTask>() + L.begin, sn, panel, F->minv.as<float>(),
                             F->stage_a.as<__nv_bfloat16>(), F->stage_b.as<__nv_bfloat16>(), D.stage.as<StageInfo>());
                     else
-                        k_panel_solve<float><<<L.count, 256, 0, st>>>(
+                        k_panel_solve<float><<<L.count, 256, kPanelSmemBytes, st>>>(
                             D.panel_tasks.as<PanelTask>() + L.begin, sn, panel, F->minv.as<float>(),
                             F->stage_a.as<float>(), F->stage_b.as<float>(), D.stage.as<StageInfo>());
                 } else {
@@ -413,6 +413,9 @@ void prepare_factor_kernels(uchol_factor_s* F) {
         CK(cudaFuncSetAttribute(k_invert_blocks<float, float, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)(2 * 128 * 128 * sizeof(float))));
         CK(cudaFuncSetAttribute(k_diag_block, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDiagSmemBytes));
+        CK(cudaFuncSetAttribute(k_panel_solve<__nv_bfloat16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)kPanelSmemBytes));
+        CK(cudaFuncSetAttribute(k_panel_solve<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPanelSmemBytes));
         CK(cudaFuncSetAttribute(k_tc_gemm<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_smem_bytes()));
         CK(cudaFuncSetAttribute(k_tc_gemm<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_smem_bytes()));
     }

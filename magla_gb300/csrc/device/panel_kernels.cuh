@@ -308,6 +308,20 @@ __global__ void __launch_bounds__(256, 1) k_diag_block(const PanelTask* __restri
     if (tid == 0) acc.flush(st);
 }
 
+// 4-byte asynchronous copy global -> shared (zero fill when !valid: nothing is read then).
+__device__ __forceinline__ void cp_async4(float* dst, const float* src, bool valid) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"((unsigned)__cvta_generic_to_shared(dst)),
+                 "l"(src), "r"(valid ? 4 : 0)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+// Shared memory of k_panel_solve: two stages of (A21 chunk, X^T chunk), 32 K columns each.
+constexpr int kPanelKc = 32, kPanelLds = kSolveRows + 4;
+constexpr size_t kPanelSmemBytes = sizeof(float) * 2 * 2 * kPanelKc * kPanelLds;
+
 __device__ __forceinline__ void store_op4(__nv_bfloat16* p, float a, float b, float c, float e) {
     __nv_bfloat162 lo = __floats2bfloat162_rn(a, b), hi = __floats2bfloat162_rn(c, e);
     uint2 v;
@@ -327,14 +341,13 @@ __device__ __forceinline__ void store_op1(float* p, float a) { *p = a; }
 // shared loads).  X^T is upper triangular, so columns below 64 take no
 // updates from K >= 64.
 template <class Op>
-__global__ void __launch_bounds__(256) k_panel_solve(const PanelTask* __restrict__ tasks,
+__global__ void __launch_bounds__(256, 2) k_panel_solve(const PanelTask* __restrict__ tasks,
                                                      const SnDev* __restrict__ sn, float* __restrict__ panel,
                                                      const float* __restrict__ minv, Op* __restrict__ stage_a,
                                                      Op* __restrict__ stage_b,
                                                      const StageInfo* __restrict__ stage_info) {
-    constexpr int KC = 32, LDS = kSolveRows + 4;
-    __shared__ __align__(16) float As[KC * LDS];
-    __shared__ __align__(16) float Ms[KC * LDS];
+    constexpr int KC = kPanelKc, LDS = kPanelLds;
+    extern __shared__ __align__(16) float psm[];   // stage s: As = psm + 2 s KC LDS, Ms = As + KC LDS
     const PanelTask tk = tasks[blockIdx.x];
     const SnDev d = sn[tk.s];
     const int nb = tk.nb, k0 = tk.j0, row0 = tk.row0, rows = tk.rows;
@@ -346,15 +359,31 @@ __global__ void __launch_bounds__(256) k_panel_solve(const PanelTask* __restrict
     for (int i = 0; i < 8; ++i)
 #pragma unroll
         for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
-    for (int kc = 0; kc < nb; kc += KC) {
-        __syncthreads();
-#pragma unroll 4
+    // K chunks of KC columns copied asynchronously into two stages: every copy of a chunk in
+    // flight at once, and the next chunk's copies under the current chunk's products
+    auto issue_chunk = [&](int kc, int st) {
+        float* As = psm + 2 * st * KC * LDS;
+        float* Ms = As + KC * LDS;
+#pragma unroll
         for (int q = 0; q < (KC * kSolveRows) / 256; ++q) {
             const int idx = tid + 256 * q, r = idx & (kSolveRows - 1), k = idx >> 7;
-            As[k * LDS + r] = (r < rows && kc + k < nb) ? A[r + (long long)(kc + k) * d.ldp] : 0.f;
-            Ms[k * LDS + r] = M[(kc + k) * kDiagMax + r];
+            const bool ok = r < rows && kc + k < nb;
+            cp_async4(&As[k * LDS + r], ok ? A + r + (long long)(kc + k) * d.ldp : A, ok);
+            cp_async4(&Ms[k * LDS + r], M + (kc + k) * kDiagMax + r, true);
+        }
+        cp_async_commit();
+    };
+    issue_chunk(0, 0);
+    for (int kc = 0, st = 0; kc < nb; kc += KC, st ^= 1) {
+        if (kc + KC < nb) {
+            issue_chunk(kc + KC, st ^ 1);
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
         }
         __syncthreads();
+        const float* As = psm + 2 * st * KC * LDS;
+        const float* Ms = As + KC * LDS;
         const bool low_cols = kc < 64;   // X^T[k][j] = 0 for j < k: columns 0..63 see K < 64 only
 #pragma unroll 4
         for (int k = 0; k < KC; ++k) {
@@ -376,6 +405,7 @@ __global__ void __launch_bounds__(256) k_panel_solve(const PanelTask* __restrict
                     for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(av[i], bl[j], acc[i][j]);
             }
         }
+        __syncthreads();   // this stage is refilled two chunks later
     }
     // epilogue: L21 = W21 D^{-1} to the factor (column-major), W21 and L21 to the staging rows (K-major)
     const float* dinv = M + kDiagMax * kDiagMax + kDiagMax;
