@@ -163,6 +163,7 @@ constexpr int kTcGroup = 8;                // column tiles per group of the tile
 constexpr int kTcEpiWarps = 8;             // two warps per TMEM lane quadrant, four 32-row chunks each
 constexpr int kTcThreads = 64 + 32 * kTcEpiWarps;   // warp 0 TMA, warp 1 MMA, warps 2-9 epilogue
 constexpr int kTcPartial = kTcCols * kTcRows;       // floats of one partial tile
+constexpr int kTcEpiLd = 33;                        // epilogue transpose buffer: 32 x 33 floats per warp
 constexpr int kTcMinSplitKb = 8;           // K blocks of a tile below which it is never split
 constexpr int kTcMaxParts = 4;             // most CTAs sharing one split tile (bounds the fixup's reads)
 
@@ -352,6 +353,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(acc_empty + 2);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
     volatile int* last_flag = reinterpret_cast<volatile int*>(tmem_slot + 2);
+    float* epi_buf = reinterpret_cast<float*>(full + 16);   // after the barriers and flags (128 bytes)
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) {
@@ -466,11 +468,34 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             const uint32_t ta = tmem + (uint32_t)(acc * kTcRows) + ((uint32_t)(q * 32) << 16);
             if (g.parts == 1) {
                 if (ok) {
+                    // the warp's 32 columns x 32 rows go through a shared-memory transpose, so that
+                    // every global access of the warp is 32 consecutive rows of one column
+                    float* tb = epi_buf + (warp - 2) * 32 * kTcEpiLd;
+                    const int jw = j0 + q * 32;   // the warp's first column
+                    const long long ld = jw < d.w ? d.ldp : d.ldc;
+                    float* colw = tc_column(panel, contrib, d, j0, jw);
 #pragma unroll 1
                     for (int cc = c_first; cc < c_first + 4; ++cc) {
                         float v[32];
                         tmem_ld32(ta + (uint32_t)(cc * 32), v);
-                        if (j < jend) tc_update_chunk(col, i0 + cc * 32, j, d.m, v);
+#pragma unroll
+                        for (int r = 0; r < 32; ++r) tb[r * kTcEpiLd + lane] = v[r];
+                        __syncwarp();
+                        const int i = i0 + cc * 32 + lane;   // this thread's row from here on
+                        if (i < d.m && i0 + cc * 32 + 31 >= jw) {
+#pragma unroll
+                            for (int h = 0; h < 32; h += 16) {   // 16 loads in flight, then their stores
+                                float o[16];
+#pragma unroll
+                                for (int c = 0; c < 16; ++c)
+                                    if (jw + h + c < jend && i >= jw + h + c) o[c] = colw[(long long)(h + c) * ld + i];
+#pragma unroll
+                                for (int c = 0; c < 16; ++c)
+                                    if (jw + h + c < jend && i >= jw + h + c)
+                                        colw[(long long)(h + c) * ld + i] = o[c] - tb[lane * kTcEpiLd + h + c];
+                            }
+                        }
+                        __syncwarp();
                     }
                 }
             } else {
@@ -600,7 +625,9 @@ inline void make_stage_maps(bool bf16, void* w_base, void* l_base, long long row
 }
 
 inline size_t tc_smem_bytes() {
-    return (size_t)kTcStages * (kTcABytes + kTcBBytes) + 1024 + (2 * kTcStages + 4) * 8 + 16;
+    static_assert((2 * kTcStages + 4) * 8 + 12 <= 128, "barriers and flags fit before the epilogue buffers");
+    return 1024 + (size_t)kTcStages * (kTcABytes + kTcBBytes) + 128 +
+           (size_t)kTcEpiWarps * 32 * kTcEpiLd * sizeof(float);
 }
 
 // Workspace of the K-split tiles: two partial tiles per CTA, one counter per split tile.
