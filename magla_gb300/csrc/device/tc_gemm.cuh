@@ -482,18 +482,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                         for (int r = 0; r < 32; ++r) tb[r * kTcEpiLd + lane] = v[r];
                         __syncwarp();
                         const int i = i0 + cc * 32 + lane;   // this thread's row from here on
+                        // each entry of C takes exactly one update per launch, so a reduction in L2
+                        // (no load, nothing to wait for) gives the same sum as a read-modify-write
                         if (i < d.m && i0 + cc * 32 + 31 >= jw) {
 #pragma unroll
-                            for (int h = 0; h < 32; h += 16) {   // 16 loads in flight, then their stores
-                                float o[16];
-#pragma unroll
-                                for (int c = 0; c < 16; ++c)
-                                    if (jw + h + c < jend && i >= jw + h + c) o[c] = colw[(long long)(h + c) * ld + i];
-#pragma unroll
-                                for (int c = 0; c < 16; ++c)
-                                    if (jw + h + c < jend && i >= jw + h + c)
-                                        colw[(long long)(h + c) * ld + i] = o[c] - tb[lane * kTcEpiLd + h + c];
-                            }
+                            for (int c = 0; c < 32; ++c)
+                                if (jw + c < jend && i >= jw + c) atomicAdd(colw + (long long)c * ld + i, -tb[lane * kTcEpiLd + c]);
                         }
                         __syncwarp();
                     }
