@@ -234,6 +234,7 @@ def run_ours(args):
     peak_bf16 = peaks.get("bf16_tflops_sustained", 1700.0)
     peak = peak_bf16 if prec == mg.Precision.BF16 else peak_bf16 / 2.0
     achieved = ph["schur_tensor_flops"] / (ph["schur_tensor_ms"] * 1e-3) / 1e12 if ph["schur_tensor_ms"] > 0 else 0.0
+    traffic = gemm_traffic(args, prec)
     fp64 = None
     if args.fp64_compare:
         f64s = mg.SymmetricUtduSolver(mg.UtduSolverOptions(Ordering=ordering, Precision=mg.Precision.FP64))
@@ -272,7 +273,7 @@ def run_ours(args):
                 "relres": e2e_relres},
         "gpu_launches": int(launches),
         "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": achieved / peak if peak else None, "traffic": None,
+                     "frac": achieved / peak if peak else None, "traffic": traffic,
                      "kernel": "k_tc_gemm", "launches_per_step": ph["schur_tensor_launches"],
                      "note": "peak = bf16_tflops_sustained of MEASURED_PEAKS.json (half of it for TF32)"},
         "phases_ms": {k: ph[k] for k in ("pivot_block_ms", "panel_ms", "schur_ms", "extend_add_ms", "small_fronts_ms",
@@ -285,6 +286,19 @@ def run_ours(args):
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+def gemm_traffic(args, prec):
+    """DRAM bytes per k_tc_gemm launch (read + write) from the committed ncu capture of this
+    workload (elasticity 40^3, BF16, AMD); None for any other configuration."""
+    import magla_gb300 as mg
+    f = ROOT / "profiles" / "k_tc_gemm_dram_elasticity40_bf16.txt"
+    if list(args.elements) != [40, 40, 40] or prec != mg.Precision.BF16 or args.ordering != "AMD" or not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        if line.startswith("traffic_bytes_per_launch:"):
+            return int(line.split(":")[1])
+    return None
 
 
 def main():
