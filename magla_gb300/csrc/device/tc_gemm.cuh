@@ -638,7 +638,7 @@ struct TcPlanned {
 };
 inline TcPlanned tc_schedule(long long tiles, int nkb, int sms) {
     TcPlanned p{(unsigned)std::max<long long>(1, std::min<long long>(tiles, sms)), tiles, 0};
-    if (nkb < kTcMinSplitKb || tiles <= 0) return p;
+    if (nkb < kTcMinSplitKb || tiles <= 0 || tiles >= sms) return p;
     const long long waves = (tiles + sms - 1) / sms;
     const double t_dp = (double)waves * nkb;
     long long G = sms;
