@@ -77,13 +77,17 @@ __device__ __forceinline__ float rcp_approx(float x) {
 // warp, with the same eliminations applied to the identity so that
 // X_bb = L_bb^{-1} comes out with it.  Lane r holds row b0 + r in registers
 // as a shift register: at pivot k, a[j] is F[r][k + j] and x[c] is X[r][c].
-// The pivot and the pivot column come by shuffles; every lane below the
-// pivot applies F[r][k+j] -= L[r][k] (d_k L[k+j][k]) (the reference's
-// association) and shifts its row by one, so the loop over pivots stays
-// rolled (short code) while every register index is a constant.  Entries
-// right of the diagonal take meaningless updates and are never read.
+// Every lane below the pivot applies F[r][k+j] -= L[r][k] (d_k L[k+j][k])
+// (the reference's association) and shifts its row by one, so the loop over
+// pivots stays rolled (short code) while every register index is a constant.
+// The pivot column (times d_k) and row k of X reach every lane through the
+// 64-float shared scratch `scr` (16-byte aligned) as eight 16-byte broadcast
+// loads each: lane r stores d_k L[r][k] at slot (r - k) mod 32, so slot j is
+// row k + j (rows above the pivot store zero).  Entries right of the
+// diagonal take meaningless updates and are never read.
 __device__ __forceinline__ void warp_ldlt32(float* S, float* X, int b0, int bn, int lane, int col0, float thr,
-                                            float reg, int allow, float* sd, float* sdi, PivotAccF& acc) {
+                                            float reg, int allow, float* sd, float* sdi, PivotAccF& acc,
+                                            float* scr) {
     float a[32], x[32];
 #pragma unroll
     for (int j = 0; j < 32; ++j) {
@@ -102,17 +106,33 @@ __device__ __forceinline__ void warp_ldlt32(float* S, float* X, int b0, int bn, 
             sd[b0 + k] = piv;
             sdi[b0 + k] = inv;
         }
+        scr[(lane - k) & 31] = piv * l;
+        if (lane == k) {
 #pragma unroll
-        for (int j = 1; j < 32; ++j) {
-            const float lj = __shfl_sync(0xffffffffu, l, (k + j) & 31);   // L[k+j][k]; wrapped lanes hold 0
-            a[j - 1] = fmaf(-l, piv * lj, a[j]);
+            for (int q = 0; q < 8; ++q)
+                reinterpret_cast<float4*>(scr + 32)[q] = make_float4(x[4 * q], x[4 * q + 1], x[4 * q + 2], x[4 * q + 3]);
         }
+        __syncwarp();
+        float pl[32], xk[32];   // d_k L[k+j][k] (zero past the block), X[k][c]
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const float4 u = reinterpret_cast<const float4*>(scr)[q];
+            const float4 v = reinterpret_cast<const float4*>(scr + 32)[q];
+            pl[4 * q] = u.x;
+            pl[4 * q + 1] = u.y;
+            pl[4 * q + 2] = u.z;
+            pl[4 * q + 3] = u.w;
+            xk[4 * q] = v.x;
+            xk[4 * q + 1] = v.y;
+            xk[4 * q + 2] = v.z;
+            xk[4 * q + 3] = v.w;
+        }
+        __syncwarp();   // the scratch is rewritten at the next pivot
+#pragma unroll
+        for (int j = 1; j < 32; ++j) a[j - 1] = fmaf(-l, pl[j], a[j]);
         a[31] = 0.f;
 #pragma unroll
-        for (int c = 0; c < 32; ++c) {
-            const float xk = __shfl_sync(0xffffffffu, x[c], k);   // X[k][c]
-            x[c] = fmaf(-l, xk, x[c]);
-        }
+        for (int c = 0; c < 32; ++c) x[c] = fmaf(-l, xk[c], x[c]);
     }
     if (lane < bn) {
 #pragma unroll
@@ -161,8 +181,9 @@ __global__ void __launch_bounds__(256, 1) k_diag_block(const PanelTask* __restri
     for (int b0 = 0; b0 < nb; b0 += 32) {
         const int bn = min(32, nb - b0);
         // (1) LDL^T of the sub-block and X_bb = L_bb^{-1}, by one warp
-        if (warp == 0)
-            warp_ldlt32(S, X, b0, bn, lane, d.first_col + k0 + b0, thr, reg, ctl.allow_regularization, sd, sdi, acc);
+        if (warp == 0)   // Wt is free until step (3): its first 64 floats are the warp's scratch
+            warp_ldlt32(S, X, b0, bn, lane, d.first_col + k0 + b0, thr, reg, ctl.allow_regularization, sd, sdi, acc,
+                        Wt);
         __syncthreads();
         // (3) rows below the sub-block: w[r][j] = sum_{k<=j} A[r][b0+k] X_bb[j][k], l = w / d_j;
         //     lane j, rows r0 + 8 q (four independent sums per lane)
