@@ -11,6 +11,7 @@
 #include <cstdio>
 #include <cstring>
 #include <type_traits>
+#include <limits>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -185,6 +186,7 @@ struct uchol_factor_s {
     size_t elem = 8;              // bytes per front element
     DBuf panel, contrib, stage_a, stage_b, diag, values, full_val, stats, ctl;
     DBuf work, fv, fv2, vec[6], scal;   // solve workspace
+    DBuf bwd_partial;                   // backward column dots split in row chunks: partial sums
     DBuf linv;                          // inverses of the diagonal blocks (solves)
     DBuf minv;                          // mixed path: per outer block X^T, D, D^{-1} of each diagonal block
     DBuf solve_flags;                   // per diagonal block: forward and backward "solution published" flags
@@ -734,7 +736,10 @@ void run_solve(uchol_factor_s* F, int nrhs, Cv* work, Cv* fv, Cv* fv2, cudaStrea
         } else if (L.kind == SolveLaunch::FwdSolo) {
             k_fwd_solo<T, Cv, SB><<<L.count, 256, 0, st>>>(tasks + L.begin, A, panel, linv, fv, fv2, diag, work);
         } else if (L.kind == SolveLaunch::FwdTail) {
-            k_fwd_tail<T, Cv, SB><<<L.count, kTailRows / 4, 0, st>>>(tasks + L.begin, A, panel, fv2, fv);
+            if (nrhs == 1)
+                k_fwd_tail<T, Cv, SB, 1><<<L.count, kTailRows / 4, 0, st>>>(tasks + L.begin, A, panel, fv2, fv);
+            else
+                k_fwd_tail<T, Cv, SB, 4><<<L.count, kTailRows / 4, 0, st>>>(tasks + L.begin, A, panel, fv2, fv);
         } else {
             const int grid = F->coop_fwd;
             launch_cooperative(k_fwd_level<T, Cv, SB>, grid, 256, smem, st, level_args(L, fwd_flags, grid), A, panel,
@@ -746,7 +751,9 @@ void run_solve(uchol_factor_s* F, int nrhs, Cv* work, Cv* fv, Cv* fv2, cudaStrea
         if (L.kind == SolveLaunch::BwdGather) {
             k_bwd_gather<Cv><<<L.count, 256, 0, st>>>(tasks + L.begin, A, work, fv);
         } else if (L.kind == SolveLaunch::BwdTail) {
-            k_bwd_cols<T, Cv><<<L.count, 256, 0, st>>>(tasks + L.begin, A, panel, fv);
+            k_bwd_cols<T, Cv><<<L.count, 256, 0, st>>>(tasks + L.begin, A, panel, fv, F->bwd_partial.as<Cv>());
+        } else if (L.kind == SolveLaunch::BwdTailReduce) {
+            k_bwd_cols_reduce<Cv><<<L.count, 128, 0, st>>>(tasks + L.begin, A, F->bwd_partial.as<Cv>(), fv);
         } else if (L.kind == SolveLaunch::BwdSolo) {
             k_bwd_solo<Cv, SB><<<L.count, 256, 0, st>>>(tasks + L.begin, A, linv, fv, fv2, work);
         } else {
@@ -844,6 +851,7 @@ void ensure_workspace(uchol_factor_s* F, int nrhs) {
     F->work.alloc((size_t)std::max(1, S->n) * nrhs * cv, "solve workspace");
     F->fv.alloc((size_t)P.fvec_elems * nrhs * cv, "solve workspace");
     F->fv2.alloc((size_t)P.fvec_elems * nrhs * cv, "solve workspace");
+    F->bwd_partial.alloc((size_t)std::max(1, P.bwd_partial_slots) * 8 * nrhs * cv, "solve workspace");
     if (F->solve_graph) {
         CK(cudaGraphExecDestroy(F->solve_graph));
         F->solve_graph = nullptr;
@@ -936,7 +944,9 @@ void solve_refined(uchol_factor_s* F, int nrhs, const double* b, int ldb, double
         double worst = 0.0;
         for (int j = 0; j < nrhs; ++j) {
             double nb = std::sqrt(hb[j]), nr = std::sqrt(hr[j]);
-            worst = std::max(worst, nb > 0.0 ? nr / nb : nr);
+            const double rel = nb > 0.0 ? nr / nb : nr;
+            if (!std::isfinite(rel)) return std::numeric_limits<double>::quiet_NaN();   // any column
+            worst = std::max(worst, rel);
         }
         return worst;
     };
@@ -951,7 +961,7 @@ void solve_refined(uchol_factor_s* F, int nrhs, const double* b, int ldb, double
     if (method == 1) {
         double* ones = sc + 15 * nrhs;
         k_fill<<<(nrhs + 31) / 32, 32, 0, st>>>(ones, 1.0, nrhs); counted();
-        while (current > opt.tolerance && it < opt.max_iterations) {
+        while (current > opt.tolerance && std::isfinite(current) && it < opt.max_iterations) {
             apply_factor(F, nrhs, r, n, z, n);
             k_axpy_cols<<<g, 256, 0, st>>>(x, ldx, z, n, ones, 1.0, n, nrhs); counted();
             residual(F, nrhs, x, ldx, b, ldb, r, n);
@@ -964,7 +974,7 @@ void solve_refined(uchol_factor_s* F, int nrhs, const double* b, int ldb, double
         apply_factor(F, nrhs, r, n, z, n);
         CK(cudaMemcpyAsync(p, z, (size_t)n * nrhs * sizeof(double), cudaMemcpyDeviceToDevice, st));
         dots(F, nrhs, r, n, z, n, rz);
-        while (current > opt.tolerance && it < opt.max_iterations) {
+        while (current > opt.tolerance && std::isfinite(current) && it < opt.max_iterations) {
             residual(F, nrhs, p, n, nullptr, 0, q, n);   // q = A p
             dots(F, nrhs, p, n, q, n, pq);
             k_cg_scalars<<<1, 32 * ((nrhs + 31) / 32), 0, st>>>(rz, pq, alpha, nrhs); counted();
@@ -987,6 +997,11 @@ void solve_refined(uchol_factor_s* F, int nrhs, const double* b, int ldb, double
     double ms = timer.stop();
     check_solve_status(F);
     if (rs) *rs = {it, current, initial, ms};
+    if (!std::isfinite(current))
+        throw Error(UCHOL_NO_CONVERGENCE,
+                    "refinement stopped after " + std::to_string(it) +
+                        " steps: the residual is not finite (a non-finite right-hand side, or a reduced-precision "
+                        "factor whose pivots broke down; refactorise with a higher precision)");
     if (current > opt.tolerance)
         throw Error(UCHOL_NO_CONVERGENCE, "refinement stopped at relative residual " + std::to_string(current) +
                                               " after " + std::to_string(it) + " steps (target " +

@@ -531,14 +531,37 @@ Plan build_plan(int n, int count, const int* first_column, const int* parent, co
         const auto& fronts = at_level[L];
         auto g = gather_tasks(fronts);
         P.bwd_launches.push_back({SolveLaunch::BwdGather, g.first, g.second, 0, 0, 0, 0, 0, 0, 0, 0, 0});
+        // column dots against the trailing rows, 8 columns per task; columns longer than
+        // kColRowsPlan rows are split into row chunks (flags = 1, blk = partial slot) whose
+        // partial sums a reduction task (k0, kn; r0 = first slot, r1 = slots) adds in order
         int tb = (int)P.solve_tasks.size();
+        std::vector<SolveBlockTask> reduce;
+        int slot = 0;
         for (int s : fronts) {
             const SnDev& d = P.sn[s];
             if (d.m == d.w) continue;
-            for (int c = 0; c < d.w; c += 8) P.solve_tasks.push_back({s, c, std::min(8, d.w - c), d.w, d.m, 0, 0});
+            const int nch = (d.m - d.w + kColRowsPlan - 1) / kColRowsPlan;
+            for (int c = 0; c < d.w; c += 8) {
+                const int kn = std::min(8, d.w - c);
+                if (nch == 1) {
+                    P.solve_tasks.push_back({s, c, kn, d.w, d.m, 0, 0});
+                    continue;
+                }
+                reduce.push_back({s, c, kn, slot, nch, 0, 0});
+                for (int q = 0; q < nch; ++q) {
+                    const int r0 = d.w + q * kColRowsPlan;
+                    P.solve_tasks.push_back({s, c, kn, r0, std::min(d.m, r0 + kColRowsPlan), 1, slot++});
+                }
+            }
         }
         if ((int)P.solve_tasks.size() > tb)
             P.bwd_launches.push_back({SolveLaunch::BwdTail, tb, (int)P.solve_tasks.size() - tb, 0, 0, 0, 0, 0, 0, 0, 0, 0});
+        if (!reduce.empty()) {
+            const int rb = (int)P.solve_tasks.size();
+            P.solve_tasks.insert(P.solve_tasks.end(), reduce.begin(), reduce.end());
+            P.bwd_launches.push_back({SolveLaunch::BwdTailReduce, rb, (int)reduce.size(), 0, 0, 0, 0, 0, 0, 0, 0, 0});
+        }
+        P.bwd_partial_slots = std::max(P.bwd_partial_slots, slot);
         SolveLaunch solo = split(fronts, multi);
         solo.kind = SolveLaunch::BwdSolo;
         if (solo.count > 0) P.bwd_launches.push_back(solo);

@@ -14,6 +14,7 @@ namespace uchol_dev {
 
 constexpr int kSolveRowsPlan = 128;   // rows per panel-solve task (kSolveRows of the kernel)
 constexpr int kTailRowsPlan = 1024;  // trailing rows per forward tail task (kTailRows of the kernel)
+constexpr int kColRowsPlan = 2048;   // trailing rows per backward column-dot task (longer columns: partial sums)
 constexpr int kSuperBlocks = 4;       // tensor-core path: outer blocks per super-block of the own-column updates
 
 struct PlanConfig {
@@ -36,7 +37,7 @@ struct Launch {
 };
 
 struct SolveLaunch {
-    enum Kind : int { FwdGather, FwdSolo, FwdLevel, BwdGather, BwdTail, BwdSolo, BwdLevel, FwdTail } kind;
+    enum Kind : int { FwdGather, FwdSolo, FwdLevel, BwdGather, BwdTail, BwdSolo, BwdLevel, FwdTail, BwdTailReduce } kind;
     int begin, count;   // tasks; level launches: the chains (one per front)
     int steps;          // level launches: most diagonal blocks of one front of the level
     int bulk_begin, bulk_count;   // level launches: the bulk chunks
@@ -104,6 +105,7 @@ struct Plan {
     std::vector<SolveBlockTask> inv_blocks;    // every diagonal block, for the inversion after a factorisation
     std::vector<SolveLaunch> fwd_launches, bwd_launches;
     int progress_count = 0;                    // progress counters of all level launches
+    int bwd_partial_slots = 0;                 // most backward column-dot partial slots of one launch (8 x nrhs each)
 };
 
 // Algorithmic flops (2 per multiply-add, lower triangle) and tiles of an update job.

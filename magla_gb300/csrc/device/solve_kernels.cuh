@@ -818,48 +818,65 @@ __device__ __forceinline__ void load4(const double* p, double* v) {
 // Forward, trailing rows of single-block fronts (after k_fwd_solo): f[i] -= sum_k L[i, k] y[k]
 // for rows [r0, r1) of the task's front (r0 a multiple of 4; rows below w are skipped).
 // Four consecutive rows per thread, one aligned group per column, eight columns in flight,
-// so a front's trailing block streams at HBM speed over many CTAs instead of one.
+// so a front's trailing block streams at HBM speed over many CTAs instead of one.  The
+// right-hand sides go in groups of G: each factor entry is read once per group.
 constexpr int kTailRows = 1024;
-template <class T, class Cv, int SB>
+template <class T, class Cv, int SB, int G>
 __global__ void __launch_bounds__(kTailRows / 4) k_fwd_tail(const SolveBlockTask* __restrict__ tasks, SolveArgs A,
                                                             const T* __restrict__ panel, const Cv* __restrict__ yv,
                                                             Cv* __restrict__ fv) {
-    __shared__ Cv y[SB];
+    __shared__ Cv y[G][SB];
     const SolveBlockTask tk = tasks[blockIdx.x];
     const SnDev d = A.sn[tk.s];
     const int w = d.w;
     const int i = tk.r0 + 4 * (int)threadIdx.x;
     const T* p = panel + d.panel_off + i;
-    for (int r = 0; r < A.nrhs; ++r) {
-        const long long base = A.fvec_off[tk.s] + r * A.fv_stride;
+    for (int r0 = 0; r0 < A.nrhs; r0 += G) {
+        const int ng = min(G, A.nrhs - r0);
         __syncthreads();
-        for (int t = threadIdx.x; t < w; t += blockDim.x) y[t] = __ldcg(yv + base + t);
+        for (int t = threadIdx.x; t < G * SB; t += blockDim.x) {
+            const int g = t / SB, kk = t - g * SB;
+            y[g][kk] = (g < ng && kk < w) ? __ldcg(yv + A.fvec_off[tk.s] + (r0 + g) * A.fv_stride + kk) : Cv(0);
+        }
         __syncthreads();
         if (i >= tk.r1) continue;
-        Cv a[4] = {Cv(0), Cv(0), Cv(0), Cv(0)};
+        Cv a[G][4];
+#pragma unroll
+        for (int g = 0; g < G; ++g)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) a[g][e] = Cv(0);
         int k = 0;
         for (; k + 8 <= w; k += 8) {
             T v[8][4];
 #pragma unroll
             for (int u = 0; u < 8; ++u) load4(p + (long long)(k + u) * d.ldp, v[u]);
 #pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                const Cv yk = y[k + u];
+            for (int u = 0; u < 8; ++u)
 #pragma unroll
-                for (int e = 0; e < 4; ++e) a[e] += (Cv)v[u][e] * yk;
-            }
+                for (int g = 0; g < G; ++g) {
+                    const Cv yk = y[g][k + u];
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) a[g][e] += (Cv)v[u][e] * yk;
+                }
         }
         for (; k < w; ++k) {
             T v[4];
             load4(p + (long long)k * d.ldp, v);
-            const Cv yk = y[k];
 #pragma unroll
-            for (int e = 0; e < 4; ++e) a[e] += (Cv)v[e] * yk;
+            for (int g = 0; g < G; ++g) {
+                const Cv yk = y[g][k];
+#pragma unroll
+                for (int e = 0; e < 4; ++e) a[g][e] += (Cv)v[e] * yk;
+            }
         }
-        Cv* f = fv + base;
 #pragma unroll
-        for (int e = 0; e < 4; ++e)
-            if (i + e >= w && i + e < tk.r1) f[i + e] -= a[e];
+        for (int g = 0; g < G; ++g) {
+            if (g >= ng) break;
+            Cv* f = fv + A.fvec_off[tk.s] + (r0 + g) * A.fv_stride;
+#pragma unroll
+            for (int e = 0; e < 4; ++e)
+                if (i + e >= w && i + e < tk.r1) f[i + e] -= a[g][e];
+        }
     }
 }
 
@@ -911,7 +928,7 @@ __global__ void k_bwd_gather(const SolveBlockTask* __restrict__ tasks, SolveArgs
 // both is aligned exactly when i is a multiple of 16 / sizeof(element).
 template <class T, class Cv>
 __global__ void k_bwd_cols(const SolveBlockTask* __restrict__ tasks, SolveArgs A, const T* __restrict__ panel,
-                           Cv* __restrict__ fv) {
+                           Cv* __restrict__ fv, Cv* __restrict__ partial) {
     static_assert(sizeof(T) == sizeof(Cv), "factor and vector elements of one size");
     constexpr int V = 16 / (int)sizeof(T);
     using Vec = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
@@ -948,7 +965,24 @@ __global__ void k_bwd_cols(const SolveBlockTask* __restrict__ tasks, SolveArgs A
         }
         for (int i = body + lane; i < tk.r1; i += 32) acc += (Cv)col[i] * g[i];
         for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        if (lane == 0) g[k] -= acc;
+        if (lane == 0) {
+            if (tk.flags) partial[((long long)tk.blk * 8 + warp) * A.nrhs + r] = acc;   // one row chunk
+            else g[k] -= acc;
+        }
+    }
+}
+
+// Columns split into row chunks: g[k] -= the chunks' partial sums, added in chunk order.
+// Task: columns [k0, k0 + kn) of front s, partial slots [r0, r0 + r1).
+template <class Cv>
+__global__ void k_bwd_cols_reduce(const SolveBlockTask* __restrict__ tasks, SolveArgs A,
+                                  const Cv* __restrict__ partial, Cv* __restrict__ fv) {
+    const SolveBlockTask tk = tasks[blockIdx.x];
+    for (int t = threadIdx.x; t < tk.kn * A.nrhs; t += blockDim.x) {
+        const int kk = t % tk.kn, r = t / tk.kn;
+        Cv sum = Cv(0);
+        for (int q = 0; q < tk.r1; ++q) sum += partial[((long long)(tk.r0 + q) * 8 + kk) * A.nrhs + r];
+        fv[A.fvec_off[tk.s] + r * A.fv_stride + tk.k0 + kk] -= sum;
     }
 }
 

@@ -271,6 +271,41 @@ def test_mixed_precision_multiple_rhs(gpu_lib):
         assert relative_residual(m, B[:, k], X[:, k]) <= 1e-10
 
 
+def test_long_trailing_columns_and_grouped_right_hand_sides(gpu_lib):
+    """Natural ordering on a flat mesh gives fronts with up to 2,271 trailing rows: their
+    backward column dots are summed in row chunks of 2,048 (then reduced in chunk order),
+    and several right-hand sides take the forward tails in groups of four."""
+    m, _ = G.elasticity(26, 26, 3)
+    opts = dict(Ordering=FillReducingOrdering.Natural)
+    sym, of = oracle_for(m, **opts)
+    B = np.stack([build_vector(m.Size, 60 + k) for k in range(5)], axis=1)
+    f = solver(**opts).Factorize(m, sym)
+    X = f.Solve(B)
+    for k in range(5):
+        assert max_relative_difference(X[:, k], of.Solve(B[:, k])) < FP64_VS_ORACLE
+    assert max_relative_difference(f.Solve(B[:, 2]), X[:, 2]) < FP64_VS_ORACLE   # one column alone
+    fm = solver(Precision=Precision.TF32, RefinementTolerance=1e-10, **opts).Factorize(m, sym)
+    Xm = fm.Solve(B)
+    for k in range(5):
+        assert relative_residual(m, B[:, k], Xm[:, k]) <= 1e-10
+
+
+def test_refinement_reports_a_non_finite_residual(gpu_lib):
+    """A NaN residual compares false against the tolerance: the refined solve must raise
+    instead of returning the NaN solution as converged."""
+    from magla_gb300.errors import RefinementNotConvergedError
+    m = G.grid_matrix(6, 6, 6, 2)
+    b = build_vector(m.Size, 11)
+    b[17] = np.nan
+    f = solver(Precision=Precision.BF16).Factorize(m)
+    with pytest.raises(RefinementNotConvergedError, match="not finite"):
+        f.SolveRefined(b, tolerance=1e-10)
+    # a finite right-hand side still converges on the same factor
+    b[17] = 0.5
+    x = f.SolveRefined(b, tolerance=1e-10)
+    assert relative_residual(m, b, x) <= 1e-10
+
+
 def test_symbolic_handle_destroyed_before_its_factor(gpu_lib):
     """A garbage collector may finalise the symbolic object first: the factor stays usable."""
     m = G.grid_matrix(6, 6, 6, 2)
