@@ -52,14 +52,24 @@ __global__ void k_permute_out(const Cv* __restrict__ work, int ldw, const int* _
 // Rows [r0, r1) of a front vector: the supernode's right-hand side (own
 // columns) plus, child by child, the child's update vector entries that map
 // into these rows (relative indices are sorted, so each child contributes a
-// contiguous range found by binary search).
-__device__ __forceinline__ int lower_bound_int(const int* a, int n, int key) {
-    int lo = 0, hi = n;
-    while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        if (a[mid] < key) lo = mid + 1; else hi = mid;
+// contiguous range, found once per child for every right-hand side).
+//
+// First index in the sorted array a[0, n) whose value is >= key, by one warp: each round
+// probes 32 evenly spaced entries and keeps the gap between the last one below the key and
+// the first one not below it (a 32-way search: three rounds for 30,000 entries).
+__device__ __forceinline__ int warp_lower_bound(const int* __restrict__ a, int n, int key, int lane) {
+    int lo = 0, hi = n;   // the answer lies in [lo, hi]
+    while (hi - lo > 32) {
+        const long long span = hi - lo;
+        const int pos = lo + (int)(span * lane / 32);
+        const int below = __popc(__ballot_sync(0xffffffffu, a[pos] < key));   // a prefix of the probes
+        const int nlo = below == 0 ? lo : lo + (int)(span * (below - 1) / 32) + 1;
+        const int nhi = below == 32 ? hi : lo + (int)(span * below / 32);
+        lo = nlo;
+        hi = nhi;
     }
-    return lo;
+    const int pos = lo + lane;
+    return lo + __popc(__ballot_sync(0xffffffffu, pos < hi && a[pos] < key));
 }
 
 template <class Cv>
@@ -69,30 +79,35 @@ __global__ void k_fwd_gather(const SolveBlockTask* __restrict__ tasks, SolveArgs
     const SolveBlockTask tk = tasks[blockIdx.x];
     const int s = tk.s;
     const SnDev d = A.sn[s];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int r = 0; r < A.nrhs; ++r) {
         Cv* f = fv + A.fvec_off[s] + r * A.fv_stride;
         for (int a = tk.r0 + threadIdx.x; a < tk.r1; a += blockDim.x)
             f[a] = a < d.w ? work[d.first_col + a + (long long)r * A.ldw] : Cv(0);
-        __syncthreads();
-        for (int c = A.child_ptr[s]; c < A.child_ptr[s + 1]; ++c) {
-            const int ch = A.children[c];
-            const SnDev cd = A.sn[ch];
-            const int t = cd.m - cd.w;
-            const int* rl = A.rel + cd.rel_off;
-            if (tk.r0 == 0 && tk.r1 == d.m) {   // the chunk is the whole front
-                if (threadIdx.x == 0) {
-                    range[0] = 0;
-                    range[1] = t;
-                }
-            } else if (threadIdx.x == 0) {
-                range[0] = lower_bound_int(rl, t, tk.r0);
-                range[1] = lower_bound_int(rl, t, tk.r1);
+    }
+    __syncthreads();
+    const bool whole = tk.r0 == 0 && tk.r1 == d.m;   // the chunk is the whole front
+    for (int c = A.child_ptr[s]; c < A.child_ptr[s + 1]; ++c) {
+        const int ch = A.children[c];
+        const SnDev cd = A.sn[ch];
+        const int t = cd.m - cd.w;
+        const int* rl = A.rel + cd.rel_off;
+        if (whole) {
+            if (threadIdx.x == 0) {
+                range[0] = 0;
+                range[1] = t;
             }
-            __syncthreads();
+        } else if (warp < 2) {   // warp 0: the chunk's first row, warp 1: its end
+            const int v = warp_lower_bound(rl, t, warp == 0 ? tk.r0 : tk.r1, lane);
+            if (lane == 0) range[warp] = v;
+        }
+        __syncthreads();
+        for (int r = 0; r < A.nrhs; ++r) {
+            Cv* f = fv + A.fvec_off[s] + r * A.fv_stride;
             const Cv* u = fv + A.fvec_off[ch] + r * A.fv_stride + cd.w;
             for (int b = range[0] + threadIdx.x; b < range[1]; b += blockDim.x) f[rl[b]] += u[b];
-            __syncthreads();
         }
+        __syncthreads();
     }
 }
 
