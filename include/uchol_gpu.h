@@ -90,6 +90,9 @@ typedef struct {
     int panel_width;                    /* PanelWidth, clamped to 4..64: pivot-block width of the FP64 path */
     int precision;                      /* UCHOL_PRECISION_* */
     int block_width;                    /* mixed paths: outer block, 64 or 128 columns (0 = 128) */
+    int small_front_buckets;            /* bit b (b < 5): fronts with 32b < m <= 32(b+1) rows are factorised
+                                           whole by one CTA in shared memory, the others by the blocked
+                                           path; 0 = the default 0x7 (m <= 96).  uchol_autotune picks it. */
 } uchol_options;
 
 /* Pivot statistics (UtduNumericFactorization.cs:57-84) and timings. */
@@ -162,6 +165,26 @@ typedef struct {
     int schur_tensor_launches;
 } uchol_phase_times;
 int uchol_factor_phase_times(uchol_factor f, uchol_phase_times* t);
+
+/* Autotuner: per front-size bucket, the kernel that factorises the fronts (one CTA with
+ * the whole front in shared memory, or the blocked path), and on the mixed paths the
+ * outer-block width (64 or 128 columns).  uchol_autotune times graph-replayed
+ * refactorisations of these values for each candidate: the default first, then one
+ * bucket toggled at a time from the largest down, each change kept when it is faster,
+ * then the other block width.  It writes the fastest options to *best (the base options
+ * with small_front_buckets and block_width set) and a report.  Every candidate builds its
+ * own factor (device memory of one factorisation at a time).  No counterpart in the
+ * reference, which has one CPU kernel per operation; the device has several shapes and
+ * the right one depends on the pattern's front sizes. */
+typedef struct {
+    int candidates;              /* configurations timed (failed ones count, with no time) */
+    double default_ms;           /* refactorisation time of the default configuration */
+    double best_ms;              /* of the chosen configuration */
+    int small_front_buckets;     /* chosen bucket mask */
+    int block_width;             /* chosen outer-block width (mixed paths; 0 on the FP64 path) */
+} uchol_autotune_report;
+int uchol_autotune(uchol_symbolic s, int n, int nnz, const double* values, const uchol_options* base,
+                   uchol_options* best, uchol_autotune_report* report);
 
 /* Device memory a factorisation with these options will reserve, computed on
  * the host from the symbolic arrays alone (no GPU needed): factor panels,

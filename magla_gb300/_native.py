@@ -62,7 +62,7 @@ class Options(C.Structure):
     _fields_ = [
         ("allow_diagonal_regularization", C.c_int), ("pivot_tolerance", C.c_double),
         ("diagonal_regularization", C.c_double), ("panel_width", C.c_int), ("precision", C.c_int),
-        ("block_width", C.c_int),
+        ("block_width", C.c_int), ("small_front_buckets", C.c_int),
     ]
 
 
@@ -72,6 +72,11 @@ class FactorStats(C.Structure):
         ("smallest_pivot_magnitude", C.c_double), ("largest_pivot_magnitude", C.c_double),
         ("failed_pivot", C.c_int), ("factor_ms", C.c_double), ("device_bytes", C.c_int64),
     ]
+
+
+class AutotuneReport(C.Structure):
+    _fields_ = [("candidates", C.c_int), ("default_ms", C.c_double), ("best_ms", C.c_double),
+                ("small_front_buckets", C.c_int), ("block_width", C.c_int)]
 
 
 class RefineOptions(C.Structure):
@@ -139,6 +144,8 @@ GPU_SYMBOLS = {
     "uchol_residual_norms_static": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                                               C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
     "uchol_residual_norms_static_error": (C.c_char_p, []),
+    "uchol_autotune": (C.c_int, [C.c_void_p, C.c_int, C.c_int, c_double_p, C.POINTER(Options), C.POINTER(Options),
+                                 C.POINTER(AutotuneReport)]),
     "uchol_kernel_launches": (C.c_int64, []),
     "uchol_set_phase_timing": (None, [C.c_int]),
     "uchol_last_error": (C.c_char_p, []),

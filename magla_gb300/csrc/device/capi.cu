@@ -143,7 +143,7 @@ struct uchol_symbolic_s {
 
     DevPlan* get_plan(const PlanConfig& c) {
         std::string key = std::to_string(c.pivot_block) + "/" + std::to_string(c.outer_block) + "/" +
-                          std::to_string(c.small_max) + "/" + std::to_string(c.tensor_core) + "/" +
+                          std::to_string(c.small_mask) + "/" + std::to_string(c.tensor_core) + "/" +
                           std::to_string(c.solve_block);
         auto it = plans.find(key);
         if (it != plans.end()) return it->second.get();
@@ -250,6 +250,7 @@ struct StreamTimer {
 
 PlanConfig config_for(const uchol_options& o) {
     PlanConfig c;
+    c.small_mask = o.small_front_buckets ? o.small_front_buckets : 0x7;
     c.pivot_block = std::min(kMaxPivotBlock, std::max(4, std::min(128, o.panel_width)));
     if (o.precision == UCHOL_PRECISION_FP64) {
         c.tensor_core = false;
@@ -402,10 +403,11 @@ void run_factor_launches(uchol_factor_s* F, cudaStream_t st) {
 }
 
 // Raises the dynamic shared-memory limits of every kernel a factorisation of
-// this configuration launches (done once, before any stream capture).
+// this configuration launches (done once, before any stream capture).  The
+// small-front kernel gets the limit of its largest bucket: the attribute is a
+// per-function maximum shared by every factor, so it never goes down.
 void prepare_factor_kernels(uchol_factor_s* F) {
-    const Plan& P = F->dp->plan;
-    const int small = (int)((size_t)P.max_small_m * P.max_small_m * sizeof(double));
+    const int small = (int)((size_t)kSmallFrontLimit * kSmallFrontLimit * sizeof(double));
     if (F->elem == 8) {
         CK(cudaFuncSetAttribute(k_small_fronts<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, std::max(small, 1)));
         CK(cudaFuncSetAttribute(k_invert_blocks<double, double, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -576,6 +578,9 @@ void check_options(const uchol_options* o) {
         throw Error(UCHOL_BAD_ARG, "unknown precision mode");
     if (!(o->pivot_tolerance >= 0.0) || !(o->diagonal_regularization > 0.0))
         throw Error(UCHOL_BAD_ARG, "pivot tolerance must be >= 0 and regularization > 0");
+    if (o->small_front_buckets < 0 || o->small_front_buckets >= (1 << kSmallBuckets))
+        throw Error(UCHOL_BAD_ARG, "small_front_buckets has bits beyond the " + std::to_string(kSmallBuckets) +
+                                       " front-size buckets");
 }
 
 uchol_factor_s* create_factor(uchol_symbolic_s* S, int n, int nnz, const uchol_options* opts) {
@@ -1026,6 +1031,7 @@ void uchol_default_options(uchol_options* o) {
     o->panel_width = 32;
     o->precision = UCHOL_PRECISION_FP64;
     o->block_width = 0;
+    o->small_front_buckets = 0;
 }
 
 int uchol_symbolic_create(const uchol_symbolic_desc* d, uchol_symbolic* out) {
@@ -1197,6 +1203,70 @@ int uchol_refactorize(uchol_factor f, const double* values, int on_device, uchol
         std::lock_guard<std::mutex> lk(f->mu);
         factorize_impl(f, values, on_device != 0);
         if (stats) *stats = f->last;
+    });
+}
+
+int uchol_autotune(uchol_symbolic s, int n, int nnz, const double* values, const uchol_options* base,
+                   uchol_options* best, uchol_autotune_report* report) {
+    return guarded([&] {
+        if (!s || !best || (!values && nnz > 0)) throw Error(UCHOL_BAD_ARG, "null argument");
+        check_options(base);
+        uchol_options o0;
+        if (base) o0 = *base; else uchol_default_options(&o0);
+        std::lock_guard<std::mutex> lk(s->mu);
+        if (n != s->n || nnz != s->nnz)
+            throw Error(UCHOL_PATTERN_MISMATCH, "the values do not match the symbolic factorization");
+        DBuf dv;
+        dv.alloc((size_t)std::max(1, nnz) * sizeof(double), "autotune values");
+        if (nnz > 0) CK(cudaMemcpy(dv.p, values, (size_t)nnz * sizeof(double), cudaMemcpyHostToDevice));
+        const bool mixed = o0.precision != UCHOL_PRECISION_FP64;
+        int candidates = 0;
+        // refactorisation time of one configuration: a factor of its own, a first factorisation
+        // (graph capture), then the best of two replays; +inf when the configuration fails
+        auto timed = [&](int mask, int bw) -> double {
+            ++candidates;
+            uchol_options o = o0;
+            o.small_front_buckets = mask;
+            o.block_width = bw;
+            try {
+                std::unique_ptr<uchol_factor_s> F(create_factor(s, n, nnz, &o));
+                factorize_impl(F.get(), dv.as<double>(), true);
+                double t = std::numeric_limits<double>::infinity();
+                for (int r = 0; r < 2; ++r) {
+                    factorize_impl(F.get(), dv.as<double>(), true);
+                    t = std::min(t, F->last.factor_ms);
+                }
+                CK(cudaStreamSynchronize(s->stream));
+                return t;
+            } catch (const Error& e) {
+                if (e.code == UCHOL_CUDA_ERROR || e.code == UCHOL_TIMEOUT) throw;   // not a property of the candidate
+                return std::numeric_limits<double>::infinity();
+            }
+        };
+        int mask = o0.small_front_buckets ? o0.small_front_buckets : 0x7;
+        int bw = mixed ? (o0.block_width > 0 ? o0.block_width : kDiagMax) : 0;
+        const double t_default = timed(mask, bw);
+        double t_best = t_default;
+        for (int b = kSmallBuckets - 1; b >= 0; --b) {
+            const int m2 = mask ^ (1 << b);
+            const double t = timed(m2, bw);
+            if (t < t_best) {
+                t_best = t;
+                mask = m2;
+            }
+        }
+        if (mixed) {
+            const int bw2 = bw == kDiagMax ? 64 : kDiagMax;
+            const double t = timed(mask, bw2);
+            if (t < t_best) {
+                t_best = t;
+                bw = bw2;
+            }
+        }
+        *best = o0;
+        best->small_front_buckets = mask;
+        best->block_width = bw;
+        if (report) *report = {candidates, t_default, t_best, mask, bw};
     });
 }
 

@@ -273,7 +273,7 @@ Plan build_plan(int n, int count, const int* first_column, const int* parent, co
         int sb = (int)P.small_fronts.size();
         std::vector<int> large;
         for (int s : fronts) {
-            if (P.sn[s].m <= cfg.small_max) {
+            if (small_front(cfg, P.sn[s].m)) {
                 P.small_fronts.push_back(s);
                 P.max_small_m = std::max(P.max_small_m, P.sn[s].m);
             } else {

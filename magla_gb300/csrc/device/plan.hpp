@@ -20,7 +20,7 @@ constexpr int kSuperBlocks = 4;       // tensor-core path: outer blocks per supe
 struct PlanConfig {
     int pivot_block = 32;     // FP64 pivot block (the reference's PanelWidth)
     int outer_block = 32;     // Schur-update block (== pivot_block on the FP64 path)
-    int small_max = 96;       // fronts with m <= small_max are factorised by one CTA in shared memory
+    int small_mask = 0x7;     // bit b: fronts with 32b < m <= 32(b+1) are factorised by one CTA in shared memory
     int tile = 64;            // SIMT tile edge (update kernels)
     bool tensor_core = false; // outer updates on tcgen05 from staged operands
     int solve_block = 64;     // column block of the triangular solves
@@ -64,6 +64,15 @@ struct TcJobHost {
     long long tile_begin;
     int s, c0, cend, kbeg, kn, map;
 };
+
+// Front-size buckets of the one-CTA small-front kernel: 32 rows each, up to kSmallFrontLimit
+// rows (the whole front in FP64 shared memory: 160^2 * 8 bytes = 200 KB).
+constexpr int kSmallBucketRows = 32;
+constexpr int kSmallFrontLimit = 160;
+constexpr int kSmallBuckets = kSmallFrontLimit / kSmallBucketRows;
+inline bool small_front(const PlanConfig& cfg, int m) {
+    return m <= kSmallFrontLimit && ((cfg.small_mask >> ((m - 1) / kSmallBucketRows)) & 1);
+}
 
 // Rows in 16 bytes of the factor storage type (float on the tensor-core path, else double):
 // tile copies by tensor map must start on a multiple of it.

@@ -20,6 +20,7 @@ block of the tensor-core update, and the refinement tolerance used by
 """
 from __future__ import annotations
 
+import copy
 import ctypes as C
 import enum
 import os
@@ -55,6 +56,7 @@ class UtduSolverOptions:
         # device extensions
         self.Precision = Precision.FP64
         self.BlockWidth = 0
+        self.SmallFrontBuckets = 0   # bit b: fronts of 32b < m <= 32(b+1) rows go whole to one CTA (0 = 0x7)
         self.RefinementTolerance = 1e-12
         self.RefinementMaxIterations = 50
         for k, v in kw.items():
@@ -77,6 +79,7 @@ class UtduSolverOptions:
         o.panel_width = int(self.ResolvePanelWidth())
         o.precision = int(self.Precision)
         o.block_width = int(self.BlockWidth)
+        o.small_front_buckets = int(self.SmallFrontBuckets)
         return o
 
 
@@ -513,6 +516,34 @@ class SymmetricUtduSolver(DirectLinearSolver):
 
     def SolveCore(self, matrix, right_hand_side):
         return self.Factorize(matrix).Solve(right_hand_side)
+
+    def Autotune(self, matrix: SymmetricCSRMatrix, symbolic: UtduSymbolicFactorization | None = None):
+        """Picks, per front-size bucket, the kernel that factorises the fronts and (mixed
+        precisions) the outer-block width, by timing refactorisations of this matrix.
+
+        Returns (options, report): a copy of this solver's options with ``SmallFrontBuckets``
+        and ``BlockWidth`` set to the fastest configuration found, and a dict with the number of
+        candidates, the default and best refactorisation times (ms) and the choices."""
+        if matrix is None:
+            raise ArgumentNullException("matrix")
+        if symbolic is None:
+            symbolic = self.Analyze(matrix)
+        else:
+            symbolic.EnsureCompatible(matrix)
+        lib = _native.gpu()
+        base = self.Options._native_options()
+        best = _native.Options()
+        rep = _native.AutotuneReport()
+        vals = np.ascontiguousarray(matrix.Values, np.float64)
+        st = lib.uchol_autotune(symbolic.device_handle(), matrix.Size, matrix.NonZeroCount,
+                                _native.ptr(vals, C.c_double), C.byref(base), C.byref(best), C.byref(rep))
+        raise_for_status(st, lib.uchol_last_error())
+        tuned = copy.copy(self.Options)
+        tuned.SmallFrontBuckets = int(best.small_front_buckets)
+        tuned.BlockWidth = int(best.block_width)
+        report = dict(candidates=rep.candidates, default_ms=rep.default_ms, best_ms=rep.best_ms,
+                      small_front_buckets=rep.small_front_buckets, block_width=rep.block_width)
+        return tuned, report
 
 
 class BatchedUtduSolver:
