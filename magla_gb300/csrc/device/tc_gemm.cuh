@@ -7,14 +7,18 @@
 // SM's operand bandwidth from L2 and HBM, not the tensor pipe, is the limit.
 // Operands arrive through TMA (128-byte swizzle) into a four-stage ring, the
 // accumulator lives in TMEM (two 256-column buffers), and eight epilogue warps
-// subtract it from the FP32 front in place: lane = column, so every thread
-// reads and writes 128 contiguous bytes of its column per 32-row chunk.
+// subtract it from the FP32 front in place: each warp's 32 columns x 32 rows go
+// through a shared-memory transpose, so that every global access of the warp
+// covers 32 consecutive rows of one column, and C takes the update as an L2
+// reduction (each entry exactly once per launch: the same sum as a
+// read-modify-write, without waiting for a load).
 //
-// Launches with few tiles are split in K (stream-K): the grid takes whole
-// tiles round robin while at least two waves remain, then divides the K
-// blocks of the remaining tiles evenly over all CTAs.  A CTA that ends with a
-// partial tile writes it to a workspace slot; the last of the tile's CTAs to
-// arrive adds the partial tiles in CTA order (deterministic) and updates C.
+// Launches with fewer tiles than SMs can be split in K (stream-K): their K
+// blocks are divided evenly over the grid.  A CTA that ends with a partial tile
+// writes it to a workspace slot; the last of the tile's CTAs to arrive adds the
+// partial tiles in CTA order (deterministic) and updates C.  The kernel also
+// takes a whole-tile prefix (TcSched::dp_tiles) before the split tiles; the
+// host schedule leaves it empty.
 //
 // Every wait on an mbarrier is bounded in time; on expiry the kernel records
 // a status word, waits once more (bounded) for its own operations, frees
@@ -629,8 +633,11 @@ inline size_t tc_ws_floats(int sms) { return (size_t)2 * sms * kTcPartial; }
 inline size_t tc_counter_count(int sms) { return (size_t)2 * sms; }
 
 // Grid and split of one launch of `tiles` tiles.  nkb: K blocks of every tile when all
-// tiles have the same K (0 otherwise: never split).  Time is counted in K blocks per CTA;
-// a split tile costs about kTcMinSplitKb more (its partial tiles through L2).
+// tiles have the same K (0 otherwise: never split).  A launch with fewer tiles than SMs is
+// split in K when that is estimated faster: time in K blocks per CTA, a split tile costing
+// about kTcMinSplitKb more (its partial tiles through L2).  Larger launches take whole
+// tiles round robin: the CTAs working on the column tiles that share W rows then stay at
+// the same K offsets, which a split tail breaks (operands read from HBM several times).
 struct TcPlanned {
     unsigned grid;
     long long dp_tiles;
@@ -639,16 +646,14 @@ struct TcPlanned {
 inline TcPlanned tc_schedule(long long tiles, int nkb, int sms) {
     TcPlanned p{(unsigned)std::max<long long>(1, std::min<long long>(tiles, sms)), tiles, 0};
     if (nkb < kTcMinSplitKb || tiles <= 0 || tiles >= sms) return p;
-    const long long waves = (tiles + sms - 1) / sms;
-    const double t_dp = (double)waves * nkb;
-    long long G = sms;
-    const long long dp = tiles >= 2LL * G ? (tiles / G - 1) * G : 0;
-    const long long W = (tiles - dp) * nkb;
-    if (dp == 0) G = std::max<long long>(1, std::min<long long>({G, W / kTcMinSplitKb, tiles * kTcMaxParts}));
-    const double t_sk = (double)(dp / G) * nkb + (double)((W + G - 1) / G) + kTcMinSplitKb;
-    if (t_sk < 0.9 * t_dp) {
+    const long long W = tiles * nkb;
+    const long long G = std::max<long long>(1, std::min<long long>({(long long)sms, W / kTcMinSplitKb,
+                                                                     tiles * kTcMaxParts}));
+    const double t_whole = nkb;   // one wave of whole tiles
+    const double t_split = (double)((W + G - 1) / G) + kTcMinSplitKb;
+    if (t_split < 0.9 * t_whole) {
         p.grid = (unsigned)G;
-        p.dp_tiles = dp;
+        p.dp_tiles = 0;
         p.sk_nkb = nkb;
     }
     return p;
