@@ -123,6 +123,51 @@ __host__ __device__ __forceinline__ long long tc_job_tiles(int c0, int cend, int
     return tc_col_prefix((cend - c0 + kTcCols - 1) / kTcCols, R0, delta);
 }
 
+// Tile t (0 <= t < tc_job_tiles) of the job with columns [c0, cend) of a front of m rows:
+// first row i0, first column j0, column limit jend.  Column tiles go in groups of
+// kTcGroup; inside a group, row tile r of every column that has one, then r + 1, so the
+// CTAs working at the same time share operand rows.  Row tile r of a column group whose
+// R_g is the first column's row-tile count is held by 2 (R_g - r) - delta of its columns
+// (all g of them for the first F rows), a prefix since R_q does not grow with q.
+constexpr int kTcGroup = 8;
+__host__ __device__ __forceinline__ void tc_decode_tile(int c0, int cend, int m, long long t, int& i0, int& j0,
+                                                        int& jend) {
+    const int nc = (cend - c0 + kTcCols - 1) / kTcCols;
+    int R0, delta;
+    tc_col_shape(c0, m, R0, delta);
+    int lo = 0, hi = (nc - 1) / kTcGroup;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (tc_col_prefix((long long)mid * kTcGroup, R0, delta) <= t) lo = mid; else hi = mid - 1;
+    }
+    t -= tc_col_prefix((long long)lo * kTcGroup, R0, delta);
+    const int g = kTcGroup < nc - lo * kTcGroup ? kTcGroup : nc - lo * kTcGroup;
+    const int Rg = R0 - lo * (kTcGroup / 2);
+    const int Fr = Rg - (g + delta + 1) / 2 + 1;
+    const int F = Fr > 0 ? Fr : 0;   // rows every column of the group has
+    int r, q;
+    if (t < (long long)F * g) {
+        r = (int)(t / g);
+        q = (int)(t % g);
+    } else {
+        t -= (long long)F * g;
+        r = F;
+        q = 0;
+        for (int guard = 0; guard < kTcGroup; ++guard, ++r) {
+            const int cr = 2 * (Rg - r) - delta;
+            const int c = cr < 0 ? 0 : (cr < g ? cr : g);
+            if (t < c) {
+                q = (int)t;
+                break;
+            }
+            t -= c;
+        }
+    }
+    j0 = c0 + (lo * kTcGroup + q) * kTcCols;
+    i0 = j0 + r * kTcRows;
+    jend = j0 + kTcCols < cend ? j0 + kTcCols : cend;
+}
+
 #ifdef __CUDACC__
 // Decodes tile t of job J (front d) for tile edge T into (i0, j0, jend).
 __device__ __forceinline__ void decode_tile(const UpdJob& J, const SnDev& d, int T, long long t, int& i0, int& j0,

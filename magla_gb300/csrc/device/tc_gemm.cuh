@@ -163,7 +163,6 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
 constexpr int kTcABytes = kTcCols * 128;   // one 128-byte K block of the L operand (columns of C)
 constexpr int kTcBBytes = kTcRows * 128;   // one 128-byte K block of the W operand (rows of C)
 constexpr int kTcStages = 4;               // shared-memory ring of (A, B) K blocks: 192 KB
-constexpr int kTcGroup = 8;                // column tiles per group of the tile order (L2 reuse)
 constexpr int kTcEpiWarps = 8;             // two warps per TMEM lane quadrant, four 32-row chunks each
 constexpr int kTcThreads = 64 + 32 * kTcEpiWarps;   // warp 0 TMA, warp 1 MMA, warps 2-9 epilogue
 constexpr int kTcPartial = kTcCols * kTcRows;       // floats of one partial tile
@@ -248,41 +247,8 @@ __device__ __forceinline__ int tc_find_job(const TcJob* __restrict__ jobs, int n
 }
 
 // Tile t of job J (front of m rows): first row i0, first column j0, column limit jend.
-// Column tiles go in groups of kTcGroup; inside a group, row tile r of every column
-// that has one, then r + 1, so the CTAs working at the same time share operand rows.
 __device__ __forceinline__ void tc_tile(const TcJob& J, int m, long long t, int& i0, int& j0, int& jend) {
-    const int nc = (J.cend - J.c0 + kTcCols - 1) / kTcCols;
-    int R0, delta;
-    tc_col_shape(J.c0, m, R0, delta);
-    int lo = 0, hi = (nc - 1) / kTcGroup;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (tc_col_prefix((long long)mid * kTcGroup, R0, delta) <= t) lo = mid; else hi = mid - 1;
-    }
-    t -= tc_col_prefix((long long)lo * kTcGroup, R0, delta);
-    const int g = min(kTcGroup, nc - lo * kTcGroup);
-    const int Rg = R0 - lo * (kTcGroup / 2);
-    const int F = max(0, Rg - (g + delta + 1) / 2 + 1);   // rows every column of the group has
-    int r, q;
-    if (t < (long long)F * g) {
-        r = (int)(t / g);
-        q = (int)(t % g);
-    } else {
-        t -= (long long)F * g;
-        r = F;
-        q = 0;
-        for (int guard = 0; guard < kTcGroup; ++guard, ++r) {
-            const int c = min(g, max(0, 2 * (Rg - r) - delta));
-            if (t < c) {
-                q = (int)t;
-                break;
-            }
-            t -= c;
-        }
-    }
-    j0 = J.c0 + (lo * kTcGroup + q) * kTcCols;
-    i0 = j0 + r * kTcRows;
-    jend = min(j0 + kTcCols, J.cend);
+    tc_decode_tile(J.c0, J.cend, m, t, i0, j0, jend);
 }
 
 // Barriers of the epilogue warps only (named barrier 1).  Every epilogue warp walks the
