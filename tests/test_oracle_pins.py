@@ -10,7 +10,8 @@ known answers held by the reference's own tests:
   strict mode failure (:601-652);
 * agreement with dense Gaussian elimination on random sparse systems (:280-301);
 * thread-count independence (:389-406) — here bitwise, since the oracle's
-  per-supernode arithmetic does not depend on the schedule.
+  per-supernode arithmetic does not depend on the schedule;
+* agreement with an iterative CG solution on the grid 7^3 (:309-328).
 """
 import numpy as np
 import pytest
@@ -143,3 +144,22 @@ def test_pivot_range_and_diagonal_against_dense_ldlt():
     assert np.allclose(f.Diagonal, d, rtol=1e-13, atol=0)
     assert f.SmallestPivotMagnitude == np.min(np.abs(d))
     assert f.LargestPivotMagnitude == np.max(np.abs(d))
+
+
+def test_grid_solution_agrees_with_conjugate_gradients():
+    """Tests/UCHOL/SymmetricUtduSolverTests.cs:309-328: the direct solution of the grid 7^3
+    (2 unknowns per node) agrees with an iterative CG solution to 1e-6.  MAGLA's own CG
+    solver is outside this build, so scipy's CG on the same matrix stands in for it."""
+    spla = pytest.importorskip("scipy.sparse.linalg")
+    m = G.grid_matrix(7, 7, 7, 2)
+    b = build_vector(m.Size, 3)
+    _, f = factor(m)
+    x = f.Solve(b)
+    A = spla.LinearOperator((m.Size, m.Size), matvec=m.Multiply, dtype=np.float64)
+    try:
+        xc, info = spla.cg(A, b, rtol=1e-12, atol=0.0, maxiter=20 * m.Size)
+    except TypeError:   # scipy before 1.12 names the tolerance tol
+        xc, info = spla.cg(A, b, tol=1e-12, atol=0.0, maxiter=20 * m.Size)
+    assert info == 0
+    assert max_relative_difference(x, xc) < 1e-6
+    assert relative_residual(m, b, x) < 1e-12
