@@ -93,6 +93,11 @@ typedef struct {
     int small_front_buckets;            /* bit b (b < 5): fronts with 32b < m <= 32(b+1) rows are factorised
                                            whole by one CTA in shared memory, the others by the blocked
                                            path; 0 = the default 0x7 (m <= 96).  uchol_autotune picks it. */
+    int chain_merge_width;              /* device fronts: runs of supernodes in which each is the only child of
+                                           the next are factorised as one front of at most this many columns
+                                           when that adds at most 5% stored entries (exact zeros); the symbolic
+                                           partition itself is unchanged.  0 = 1024, < 0 = one front per
+                                           supernode. */
 } uchol_options;
 
 /* Pivot statistics (UtduNumericFactorization.cs:57-84) and timings. */

@@ -62,7 +62,7 @@ class Options(C.Structure):
     _fields_ = [
         ("allow_diagonal_regularization", C.c_int), ("pivot_tolerance", C.c_double),
         ("diagonal_regularization", C.c_double), ("panel_width", C.c_int), ("precision", C.c_int),
-        ("block_width", C.c_int), ("small_front_buckets", C.c_int),
+        ("block_width", C.c_int), ("small_front_buckets", C.c_int), ("chain_merge_width", C.c_int),
     ]
 
 

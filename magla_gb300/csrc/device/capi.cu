@@ -116,6 +116,7 @@ struct DevPlan {
     DBuf sn, rel, asm_pos, ea_items, ea_entries, small, pivot_tasks, panel_tasks, simt_jobs, tc_jobs,
         stage;
     DBuf fvec_off, solve_fronts, solve_tasks, inv_blocks;
+    DBuf rows, child_ptr, children;   // structure of the device fronts
 };
 
 inline int grid_for(long long work, int block, int cap = 152 * 16) {
@@ -136,7 +137,7 @@ struct uchol_symbolic_s {
     // host copies of the symbolic arrays (plans are built lazily per configuration)
     std::vector<int> row_ptr, col, perm, diag_idx, pat_ptr, pat_rows, lower_start, lower_ptr, lower_idx;
     std::vector<int> first_col, parent, child_ptr, children, front_ptr, front_rows;
-    DBuf d_perm, d_diag_idx, d_rows, d_child_ptr, d_children, d_full_ptr, d_full_col, d_full_src;
+    DBuf d_perm, d_diag_idx, d_full_ptr, d_full_col, d_full_src;
     long long full_nnz = 0;
     std::map<std::string, std::unique_ptr<DevPlan>> plans;
     std::mutex mu;
@@ -144,7 +145,8 @@ struct uchol_symbolic_s {
     DevPlan* get_plan(const PlanConfig& c) {
         std::string key = std::to_string(c.pivot_block) + "/" + std::to_string(c.outer_block) + "/" +
                           std::to_string(c.small_mask) + "/" + std::to_string(c.tensor_core) + "/" +
-                          std::to_string(c.solve_block);
+                          std::to_string(c.solve_block) + "/" + std::to_string(c.merge_cols) + "/" +
+                          std::to_string(c.merge_fill);
         auto it = plans.find(key);
         if (it != plans.end()) return it->second.get();
         auto dp = std::make_unique<DevPlan>();
@@ -171,6 +173,9 @@ struct uchol_symbolic_s {
         dp->solve_fronts.upload(P.solve_fronts, stream, "plan");
         dp->solve_tasks.upload(P.solve_tasks, stream, "plan");
         dp->inv_blocks.upload(P.inv_blocks, stream, "plan");
+        dp->rows.upload(P.front_rows, stream, "front rows");
+        dp->child_ptr.upload(P.child_ptr, stream, "children");
+        dp->children.upload(P.children, stream, "children");
         CK(cudaStreamSynchronize(stream));
         DevPlan* raw = dp.get();
         plans[key] = std::move(dp);
@@ -252,6 +257,7 @@ PlanConfig config_for(const uchol_options& o) {
     PlanConfig c;
     c.small_mask = o.small_front_buckets ? o.small_front_buckets : 0x7;
     c.pivot_block = std::min(kMaxPivotBlock, std::max(4, std::min(128, o.panel_width)));
+    c.merge_cols = o.chain_merge_width == 0 ? kDefaultMergeCols : std::max(0, o.chain_merge_width);
     if (o.precision == UCHOL_PRECISION_FP64) {
         c.tensor_core = false;
         c.outer_block = c.pivot_block;
@@ -684,9 +690,9 @@ void run_solve(uchol_factor_s* F, int nrhs, Cv* work, Cv* fv, Cv* fv2, cudaStrea
     SolveArgs A;
     A.sn = D.sn.as<SnDev>();
     A.rel = D.rel.as<int>();
-    A.rows = S->d_rows.as<int>();
-    A.child_ptr = S->d_child_ptr.as<int>();
-    A.children = S->d_children.as<int>();
+    A.rows = D.rows.as<int>();
+    A.child_ptr = D.child_ptr.as<int>();
+    A.children = D.children.as<int>();
     A.fvec_off = D.fvec_off.as<long long>();
     A.fv_stride = P.fvec_elems;
     A.n = S->n;
@@ -1032,6 +1038,7 @@ void uchol_default_options(uchol_options* o) {
     o->precision = UCHOL_PRECISION_FP64;
     o->block_width = 0;
     o->small_front_buckets = 0;
+    o->chain_merge_width = 0;
 }
 
 int uchol_symbolic_create(const uchol_symbolic_desc* d, uchol_symbolic* out) {
@@ -1110,9 +1117,6 @@ int uchol_symbolic_create(const uchol_symbolic_desc* d, uchol_symbolic* out) {
             }
             S->d_perm.upload(S->perm, S->stream, "permutation");
             S->d_diag_idx.upload(S->diag_idx, S->stream, "diagonal indices");
-            S->d_rows.upload(S->front_rows, S->stream, "front rows");
-            S->d_child_ptr.upload(S->child_ptr, S->stream, "children");
-            S->d_children.upload(S->children, S->stream, "children");
             build_full_csr(S.get());
             CK(cudaStreamSynchronize(S->stream));
         }

@@ -89,17 +89,11 @@ long long job_tiles(const UpdJob& J, const SnDev& d, int T) {
 }
 
 
-Plan build_plan(int n, int count, const int* first_column, const int* parent, const int* child_ptr,
-                const int* children, const int* front_ptr, const int* front_rows, const int* diag_value_index,
-                const int* pattern_ptr, const int* pattern_rows, const int* lower_start, const int* lower_value_ptr,
-                const int* lower_value_index, int nnz, const PlanConfig& cfg) {
-    Plan P;
-    P.cfg = cfg;
-    P.n = n;
-    P.count = count;
-    if (count == 0) return P;
+namespace {
 
-    // ---- validation of the symbolic input (every device index is checked here) ----
+// Checks the front structure (every device index the plan derives from it).
+void validate_fronts(int n, int count, const int* first_column, const int* parent, const int* child_ptr,
+                     const int* children, const int* front_ptr, const int* front_rows) {
     if (first_column[0] != 0 || first_column[count] != n) fail("first_column does not span 0..n");
     if (front_ptr[0] != 0) fail("front_ptr must start at 0");
     for (int s = 0; s < count; ++s) {
@@ -118,6 +112,18 @@ Plan build_plan(int n, int count, const int* first_column, const int* parent, co
         for (int c = child_ptr[s]; c < child_ptr[s + 1]; ++c)
             if (children[c] < 0 || children[c] >= s || parent[children[c]] != s) fail("children list inconsistent with parents");
     }
+}
+
+Plan build_from_fronts(int n, int count, const int* first_column, const int* parent, const int* child_ptr,
+                       const int* children, const int* front_ptr, const int* front_rows, const int* diag_value_index,
+                       const int* pattern_ptr, const int* pattern_rows, const int* lower_start,
+                       const int* lower_value_ptr, const int* lower_value_index, int nnz, const PlanConfig& cfg) {
+    Plan P;
+    P.cfg = cfg;
+    P.n = n;
+    P.count = count;
+    if (count == 0) return P;
+    validate_fronts(n, count, first_column, parent, child_ptr, children, front_ptr, front_rows);
     if ((long long)pattern_ptr[n] < 0 || lower_value_ptr[n] < 0) fail("negative pattern length");
 
     // ---- levels (height in the assembly tree) ----
@@ -567,6 +573,82 @@ Plan build_plan(int n, int count, const int* first_column, const int* parent, co
         if (solo.count > 0) P.bwd_launches.push_back(solo);
         if (!multi.empty()) P.bwd_launches.push_back(level_launch(SolveLaunch::BwdLevel, multi, false));
     }
+    return P;
+}
+
+}  // namespace
+
+FrontStructure merge_chains(int n, int count, const int* first_column, const int* parent, const int* child_ptr,
+                            const int* children, const int* front_ptr, const int* front_rows, int max_cols,
+                            double max_fill) {
+    FrontStructure F;
+    F.group_of.assign(count, 0);
+    // lower-trapezoid entries of a front of m rows and w columns
+    auto entries = [](long long m, long long w) { return (double)(w * m - w * (w - 1) / 2); };
+    std::vector<std::pair<int, int>> groups;   // first and last member
+    for (int a = 0; a < count;) {
+        int e = a;
+        double own = entries(front_ptr[a + 1] - front_ptr[a], first_column[a + 1] - first_column[a]);
+        while (max_cols > 0) {
+            const int p = parent[e];
+            if (p != e + 1 || child_ptr[p + 1] - child_ptr[p] != 1) break;   // not the next supernode's only child
+            const int wg = first_column[p + 1] - first_column[a];
+            if (wg > max_cols) break;
+            const int wp = first_column[p + 1] - first_column[p], mp = front_ptr[p + 1] - front_ptr[p];
+            const double with_p = own + entries(mp, wp);
+            if (entries(wg + (mp - wp), wg) > (1.0 + max_fill) * with_p) break;
+            own = with_p;
+            e = p;
+        }
+        for (int q = a; q <= e; ++q) F.group_of[q] = (int)groups.size();
+        groups.push_back({a, e});
+        a = e + 1;
+    }
+    F.count = (int)groups.size();
+    F.first_column.resize(F.count + 1);
+    F.parent.resize(F.count);
+    F.child_ptr.assign(F.count + 1, 0);
+    F.front_ptr.assign(F.count + 1, 0);
+    for (int g = 0; g < F.count; ++g) {
+        const int a = groups[g].first, e = groups[g].second;
+        F.first_column[g] = first_column[a];
+        F.parent[g] = parent[e] < 0 ? -1 : F.group_of[parent[e]];
+        // the group's columns, then the last member's trailing rows
+        for (int c = first_column[a]; c < first_column[e + 1]; ++c) F.front_rows.push_back(c);
+        const int we = first_column[e + 1] - first_column[e];
+        F.front_rows.insert(F.front_rows.end(), front_rows + front_ptr[e] + we, front_rows + front_ptr[e + 1]);
+        F.front_ptr[g + 1] = (int)F.front_rows.size();
+        // children from outside the group: those of its first member (each later member's only
+        // child is the member before it); ascending, as group numbers follow supernode numbers
+        for (int c = child_ptr[a]; c < child_ptr[a + 1]; ++c) F.children.push_back(F.group_of[children[c]]);
+        F.child_ptr[g + 1] = (int)F.children.size();
+    }
+    F.first_column[F.count] = count > 0 ? first_column[count] : 0;
+    (void)n;
+    return F;
+}
+
+Plan build_plan(int n, int count, const int* first_column, const int* parent, const int* child_ptr,
+                const int* children, const int* front_ptr, const int* front_rows, const int* diag_value_index,
+                const int* pattern_ptr, const int* pattern_rows, const int* lower_start, const int* lower_value_ptr,
+                const int* lower_value_index, int nnz, const PlanConfig& cfg) {
+    if (count == 0) {
+        Plan P;
+        P.cfg = cfg;
+        P.n = n;
+        P.child_ptr.assign(1, 0);
+        return P;
+    }
+    validate_fronts(n, count, first_column, parent, child_ptr, children, front_ptr, front_rows);
+    FrontStructure F = merge_chains(n, count, first_column, parent, child_ptr, children, front_ptr, front_rows,
+                                    cfg.merge_cols, cfg.merge_fill);
+    Plan P = build_from_fronts(n, F.count, F.first_column.data(), F.parent.data(), F.child_ptr.data(),
+                               F.children.data(), F.front_ptr.data(), F.front_rows.data(), diag_value_index,
+                               pattern_ptr, pattern_rows, lower_start, lower_value_ptr, lower_value_index, nnz, cfg);
+    P.supernodes = count;
+    P.front_rows = std::move(F.front_rows);
+    P.child_ptr = std::move(F.child_ptr);
+    P.children = std::move(F.children);
     return P;
 }
 

@@ -16,6 +16,7 @@ constexpr int kSolveRowsPlan = 128;   // rows per panel-solve task (kSolveRows o
 constexpr int kTailRowsPlan = 1024;  // trailing rows per forward tail task (kTailRows of the kernel)
 constexpr int kColRowsPlan = 2048;   // trailing rows per backward column-dot task (longer columns: partial sums)
 constexpr int kSuperBlocks = 4;       // tensor-core path: outer blocks per super-block of the own-column updates
+constexpr int kDefaultMergeCols = 1024;   // widest device front made of a chain of supernodes (merge_chains)
 
 struct PlanConfig {
     int pivot_block = 32;     // FP64 pivot block (the reference's PanelWidth)
@@ -24,7 +25,27 @@ struct PlanConfig {
     int tile = 64;            // SIMT tile edge (update kernels)
     bool tensor_core = false; // outer updates on tcgen05 from staged operands
     int solve_block = 64;     // column block of the triangular solves
+    int merge_cols = 0;       // > 0: single-child chains of supernodes grouped into device fronts of at most
+                              // this many columns (see merge_chains); 0: one device front per supernode
+    double merge_fill = 0.05; // largest growth of the stored entries a grouping may cost
 };
+
+// Device fronts from the supernode partition: runs of supernodes in which each
+// one is the only child of the next are grouped into one front, as long as the
+// group stays within cfg.merge_cols columns and its lower-trapezoid entries
+// exceed the members' own by at most cfg.merge_fill.  A group's rows are its
+// columns followed by the last member's trailing rows (every earlier member's
+// trailing rows outside the group are among them), so the group is a valid
+// front of the same elimination order: the entries it adds are structural zeros
+// that stay exactly zero, and its parent's front contains its trailing rows.
+struct FrontStructure {
+    int count = 0;
+    std::vector<int> first_column, parent, child_ptr, children, front_ptr, front_rows;
+    std::vector<int> group_of;   // per supernode: its device front
+};
+FrontStructure merge_chains(int n, int count, const int* first_column, const int* parent, const int* child_ptr,
+                            const int* children, const int* front_ptr, const int* front_rows, int max_cols,
+                            double max_fill);
 
 // One kernel launch: a contiguous range of tasks in one of the task arrays.
 struct Launch {
@@ -80,7 +101,9 @@ inline int kTileAlignRows(const PlanConfig& cfg) { return cfg.tensor_core ? 4 : 
 
 struct Plan {
     PlanConfig cfg;
-    int n = 0, count = 0, levels = 0;
+    int n = 0, count = 0, levels = 0;          // count: device fronts
+    int supernodes = 0;                        // supernodes of the symbolic partition
+    std::vector<int> front_rows, child_ptr, children;   // structure of the device fronts (solves)
     std::vector<int> level_of;                 // per supernode
     std::vector<SnDev> sn;                     // per supernode
     std::vector<int> rel;                      // parent-local index of each trailing row

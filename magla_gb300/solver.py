@@ -57,6 +57,7 @@ class UtduSolverOptions:
         self.Precision = Precision.FP64
         self.BlockWidth = 0
         self.SmallFrontBuckets = 0   # bit b: fronts of 32b < m <= 32(b+1) rows go whole to one CTA (0 = 0x7)
+        self.ChainMergeWidth = 0     # widest device front grouped from a chain of supernodes (0 = 1024, < 0 = off)
         self.RefinementTolerance = 1e-12
         self.RefinementMaxIterations = 50
         for k, v in kw.items():
@@ -80,6 +81,7 @@ class UtduSolverOptions:
         o.precision = int(self.Precision)
         o.block_width = int(self.BlockWidth)
         o.small_front_buckets = int(self.SmallFrontBuckets)
+        o.chain_merge_width = int(self.ChainMergeWidth)
         return o
 
 
