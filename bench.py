@@ -1,21 +1,32 @@
 #!/usr/bin/env python
 """Benchmark of the GPU numeric phase of the UCHOL direct solver.
 
-Workload (default): 3D linear elasticity, Q1 hexahedra on 40 x 40 x 40 unit
-elements (206,763 equations), E = 1, nu = 0.3, face z = 0 clamped with the
-reference's LineCross semantics, the reference's default AMD ordering.
-Right-hand side: consistent load of a unit body force plus uniform[-0.1, 0.1]
-noise (seeded).  Synthetic data; no external dataset.
+Workload (default): the large refactorisation case.  3D linear elasticity,
+Q1 hexahedra on 80 x 80 x 40 unit elements (807,003 equations), nu = 0.3,
+face z = 0 clamped with the reference's LineCross semantics, natural
+ordering (the reference's AMD ordering overflows its 32-bit factor layout
+on this mesh).  Young's modulus per element is 1 x (1 + uniform[-0.05, 0.05]),
+drawn afresh for each of 10 value sets with the sparsity pattern fixed; step
+k refactorises value set k mod 10.  16 right-hand sides, each the consistent
+load of a unit body force plus uniform[-0.1, 0.1] noise.  All seeded
+synthetic data; no external dataset.
 
-One step = numeric factorisation (mixed precision: BF16 tensor-core Schur
-updates with FP32 accumulation, FP32 fronts and pivot blocks) + solve refined
-with the FP64 residual product until ||b - Ax|| / ||b|| <= 1e-10.
+One step = numeric refactorisation (graph replay; TF32 tensor-core Schur
+updates with FP32 accumulation, FP32 fronts) + the 16-column solve refined
+with the FP64 residual product until every column has
+||b - Ax|| / ||b|| <= 1e-10.
 
 metric value: the reference's FactorOperationCount divided by the time of
 factorisation + refined solve (TFLOP/s), inputs resident in HBM.
 e2e: the same through the public API (SymmetricUtduSolver refactorisation and
 Solve) with host buffers: matrix values and b copied in, x copied out.
-Inputs exceed L2 (factor 17.9 GB), so no L2 flush is needed between steps.
+fp64_gpu: the plain FP64 GPU factorisation + solve of value set 0 (its
+device time, graph capture excluded), the mixed arm's speed-up over it, and
+the forward error of the mixed solution of value set 0 against it.
+Inputs exceed L2 (factor 67 GB), so no L2 flush is needed between steps.
+
+--elements 40 40 40 --ordering AMD --precision BF16 --nrhs 1 --perturbations 0
+gives the 206,763-equation elasticity case with E = 1.
 
 --impl reference: the reference's CPU algorithm (the C++ port in oracle/,
 all host threads) on a bounded sample of the workload.
@@ -45,19 +56,26 @@ def parse():
     p.add_argument("--steps", type=int, default=3)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--elements", type=int, nargs=3, default=[40, 40, 40])
-    p.add_argument("--precision", default="BF16", choices=["BF16", "TF32", "FP64"])
-    p.add_argument("--ordering", default="AMD", choices=["AMD", "Natural"])
+    p.add_argument("--elements", type=int, nargs=3, default=[80, 80, 40])
+    p.add_argument("--precision", default="TF32", choices=["BF16", "TF32", "FP64"])
+    p.add_argument("--ordering", default="Natural", choices=["AMD", "Natural"])
+    p.add_argument("--nrhs", type=int, default=16, help="right-hand sides per solve")
+    p.add_argument("--perturbations", type=int, default=10,
+                   help="value sets with E = 1 + uniform[-0.05, 0.05] per element (0: E = 1 throughout)")
     p.add_argument("--tol", type=float, default=1e-10)
-    p.add_argument("--fp64-compare", action="store_true", help="also time the plain FP64 factor+solve once")
-    p.add_argument("--fp64-first", action="store_true",
-                   help="time the FP64 arm's first factorisation (one-time graph capture included) instead of "
-                        "a refactorisation after it: halves the FP64 arm's GPU time on the largest workloads")
-    p.add_argument("--cpu-sample-elements", type=int, default=20)
+    p.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 GPU arm")
+    p.add_argument("--cpu-sample-elements", type=int, nargs=3, default=None,
+                   help="mesh of the CPU baseline sample (default: 0.3 x the workload's mesh, at least 8)")
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--nrhs", type=int, default=1, help="right-hand sides per solve (the refactorisation "
-                   "workload of 80x80x40 elements, natural ordering, takes 16)")
     return p.parse_args()
+
+
+def cpu_sample_elements(args):
+    if args.cpu_sample_elements:
+        return list(args.cpu_sample_elements)
+    if args.ordering == "AMD":
+        return [20, 20, 20]
+    return [max(8, int(round(e * 0.3))) for e in args.elements]
 
 
 class ClockSampler:
@@ -108,23 +126,37 @@ class ClockSampler:
 
 
 def make_workload(args):
+    """Matrix (pattern of value set 0), the value sets, and the n x nrhs right-hand sides."""
     from magla_gb300 import generators as G
     ex, ey, ez = args.elements
-    m, load = G.elasticity(ex, ey, ez)
     rng = np.random.default_rng(20260812)
+    sets = []
+    if args.perturbations > 0:
+        m = load = None
+        for k in range(args.perturbations):
+            E = 1.0 + rng.uniform(-0.05, 0.05, ex * ey * ez)
+            mk, lk = G.elasticity(ex, ey, ez, youngs=E)
+            if m is None:
+                m, load = mk, lk
+            elif mk.NonZeroCount != m.NonZeroCount or not np.array_equal(mk.ColumnIndices, m.ColumnIndices):
+                raise RuntimeError("a value perturbation changed the sparsity pattern")
+            sets.append(np.ascontiguousarray(mk.Values))
+    else:
+        m, load = G.elasticity(ex, ey, ez)
+        sets.append(np.ascontiguousarray(m.Values))
     # n x nrhs block (column-major): unit body force plus uniform[-0.1, 0.1] noise per column
     b = np.asfortranarray(np.stack([load + rng.uniform(-0.1, 0.1, m.Size) for _ in range(args.nrhs)], axis=1))
-    return m, (b[:, 0].copy() if args.nrhs == 1 else b)
+    return m, sets, b
 
 
 def cpu_baseline(args, threads):
     """The oracle (C++ port of the reference's numeric phase) on a bounded sample:
-    the same mesh family at --cpu-sample-elements^3, all host threads."""
+    the same mesh family and ordering on a smaller mesh, all host threads."""
     import oracle
     import magla_gb300 as mg
     from magla_gb300 import generators as G
-    e = args.cpu_sample_elements
-    m, load = G.elasticity(e, e, e)
+    e = cpu_sample_elements(args)
+    m, load = G.elasticity(*e)
     b = load + np.random.default_rng(20260812).uniform(-0.1, 0.1, m.Size)
     opts = mg.UtduSolverOptions(Ordering=mg.FillReducingOrdering[
         "ApproximateMinimumDegree" if args.ordering == "AMD" else "Natural"])
@@ -135,8 +167,9 @@ def cpu_baseline(args, threads):
     dt = time.perf_counter() - t
     rr = oracle.residual_norm(m, b, x) / np.linalg.norm(b)
     return {"value": sym.FactorOperationCount / dt / 1e12, "unit": "TFLOP/s", "cores": threads, "kind": "port",
-            "sample": f"elasticity {e}^3 elements (n={m.Size}, FactorOperationCount={sym.FactorOperationCount:.3e}), "
-                      f"factor+solve {dt:.2f} s, relres {rr:.1e}"}
+            "sample": f"elasticity {e[0]}x{e[1]}x{e[2]} elements, {args.ordering} ordering (n={m.Size}, "
+                      f"FactorOperationCount={sym.FactorOperationCount:.3e}), factor+solve of one right-hand "
+                      f"side {dt:.2f} s, relres {rr:.1e}"}
 
 
 def run_reference(args):
@@ -152,14 +185,19 @@ def run_reference(args):
             vals.append(cb["value"])
     v = float(np.median(vals)) if vals else cb["value"]
     cb["value"] = v
+    e = cpu_sample_elements(args)
     line = {"metric": METRIC, "value": v, "unit": "TFLOP/s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "higher_is_better": True, "impl": "reference",
-            "config": {"workload": f"elasticity Q1 {args.cpu_sample_elements}^3 elements (bounded sample of "
+            "config": {"workload": f"elasticity Q1 {e[0]}x{e[1]}x{e[2]} elements (bounded sample of "
                                    f"{args.elements[0]}x{args.elements[1]}x{args.elements[2]})",
                        "ordering": args.ordering},
             "dtype": "f64", "data": "synthetic", "cpu_baseline": cb,
             "e2e": {"value": v, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def _cols(b):
+    return b.reshape(b.shape[0], -1)
 
 
 def run_ours(args):
@@ -176,7 +214,8 @@ def run_ours(args):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
-    m, b = make_workload(args)
+    m, sets, b = make_workload(args)
+    nrhs = args.nrhs
     ordering = mg.FillReducingOrdering["ApproximateMinimumDegree" if args.ordering == "AMD" else "Natural"]
     prec = mg.Precision[args.precision]
     opts = mg.UtduSolverOptions(Ordering=ordering, Precision=prec, RefinementTolerance=args.tol,
@@ -188,58 +227,88 @@ def run_ours(args):
     stream = torch.cuda.current_stream()
     sym.SetStream(stream.cuda_stream)
     ops = sym.FactorOperationCount
-    d_vals = torch.from_numpy(np.ascontiguousarray(m.Values)).cuda()
-    nrhs = args.nrhs
-    # column-major n x nrhs device blocks (a transposed contiguous tensor)
-    d_b = torch.from_numpy(np.ascontiguousarray(b.T if nrhs > 1 else b)).cuda()
-    d_x = torch.zeros_like(d_b)
-    f = solver.Factorize(m, sym)
     lib = _native.gpu()
+    d_sets = [torch.from_numpy(v).cuda() for v in sets]
+    # column-major n x nrhs device blocks (a transposed contiguous tensor)
+    d_b = torch.from_numpy(np.ascontiguousarray(b.T)).cuda()
+    d_x = torch.zeros_like(d_b)
+    bnorm = np.linalg.norm(_cols(b), axis=0)
 
-    def step():
-        f.RefactorizeDevice(d_vals.data_ptr())
+    # ---- plain FP64 GPU arm: factorisation (device time; graph capture excluded) + one solve
+    fp64 = None
+    x64 = None
+    if not args.no_fp64 and prec != mg.Precision.FP64:
+        s64 = mg.SymmetricUtduSolver(mg.UtduSolverOptions(Ordering=ordering, Precision=mg.Precision.FP64))
+        f64 = s64.FactorizeDevice(m, sym, d_sets[0].data_ptr())
+        factor64_s = f64.FactorMilliseconds / 1e3
+        f64.SolveDevice(d_b.data_ptr(), d_x.data_ptr(), nrhs)   # first call captures the solve graph
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        f64.SolveDevice(d_b.data_ptr(), d_x.data_ptr(), nrhs)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        solve64_s = e0.elapsed_time(e1) / 1e3
+        x64 = d_x.cpu().numpy().T.copy()
+        rr64 = float(np.max(f64.DeviceResidualNorms(b, x64) / bnorm))
+        fp64 = {"factor_s": factor64_s, "solve_s": solve64_s, "factor_solve_s": factor64_s + solve64_s,
+                "tflops": ops / (factor64_s + solve64_s) / 1e12, "relres": rr64,
+                "timed": "factorisation (device time, capture excluded) + one solve of all right-hand sides"}
+        del f64
+        torch.cuda.synchronize()
+
+    # ---- mixed arm
+    f = solver.FactorizeDevice(m, sym, d_sets[0].data_ptr())
+
+    def step(k):
+        f.RefactorizeDevice(d_sets[k % len(d_sets)].data_ptr())
         return f.SolveRefinedDevice(d_b.data_ptr(), d_x.data_ptr(), nrhs, args.tol, 200)
 
-    for _ in range(args.warmup):
-        step()
+    for k in range(args.warmup):
+        step(k)
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
     launches0 = lib.uchol_kernel_launches()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    iters = []
+    iters, relres_steps = [], []
     with ClockSampler(local) as clocks:
         torch.cuda.synchronize()
         ev0.record(stream)
-        for _ in range(args.steps):
-            rs = step()
+        for k in range(args.steps):
+            rs = step(k)
             iters.append(rs.iterations)
+            relres_steps.append(rs.relative_residual)
         ev1.record(stream)
         torch.cuda.synchronize()
     launches = lib.uchol_kernel_launches() - launches0
     ms = max_over_ranks(ev0.elapsed_time(ev1) / args.steps)   # replicas: the slowest rank defines the step
-    def worst_relres(fac, x_host):
-        X = x_host.T if nrhs > 1 else x_host
-        return float(np.max(fac.DeviceResidualNorms(b, X) / np.linalg.norm(b.reshape(m.Size, -1), axis=0)))
+    # accuracy of value set 0: the library's FP64 residual, and the forward error against the FP64 arm
+    step(0)
+    torch.cuda.synchronize()
+    x0 = d_x.cpu().numpy().T.copy()
+    relres0 = float(np.max(f.DeviceResidualNorms(b, x0) / bnorm))
+    fwd_err = None
+    if x64 is not None:
+        fwd_err = float(np.max(np.linalg.norm(_cols(x0 - x64), axis=0) / np.linalg.norm(_cols(x64), axis=0)))
+        fp64["speedup_mixed_vs_fp64"] = fp64["factor_solve_s"] / (ms / 1e3)
 
-    relres = worst_relres(f, d_x.cpu().numpy())
-
-    # end to end through the public API with host buffers
-    e2e_ms = []
-    for i in range(args.warmup + args.steps):
+    # ---- end to end through the public API with host buffers (values and b in, x out)
+    mats = [_with_values(m, v) for v in sets]
+    e2e_ms, e2e_rr = [], []
+    for k in range(args.steps):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        f.Refactorize(m)
+        f.Refactorize(mats[k % len(mats)])
         x_host = f.Solve(b)
         torch.cuda.synchronize()
-        if i >= args.warmup:
-            e2e_ms.append((time.perf_counter() - t0) * 1e3)
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+        e2e_rr.append(f.LastRefinement.relative_residual if f.LastRefinement is not None else None)
     e2e = float(np.mean(e2e_ms))
-    e2e_relres = float(np.max(f.DeviceResidualNorms(b, x_host) / np.linalg.norm(b.reshape(m.Size, -1), axis=0)))
 
-    # roofline of the dominant kernel: one instrumented factorisation after the timed steps
+    # ---- roofline of the dominant kernel: one instrumented factorisation and solve after the timed steps
     lib.uchol_set_phase_timing(1)
-    f.RefactorizeDevice(d_vals.data_ptr())
+    f.RefactorizeDevice(d_sets[0].data_ptr())
+    f.SolveDevice(d_b.data_ptr(), d_x.data_ptr(), nrhs)
     lib.uchol_set_phase_timing(0)
     ph = f.PhaseTimes()
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
@@ -247,55 +316,45 @@ def run_ours(args):
     peak = peak_bf16 if prec == mg.Precision.BF16 else peak_bf16 / 2.0
     achieved = ph["schur_tensor_flops"] / (ph["schur_tensor_ms"] * 1e-3) / 1e12 if ph["schur_tensor_ms"] > 0 else 0.0
     traffic = gemm_traffic(args, prec)
-    fp64 = None
-    if args.fp64_compare:
-        f64s = mg.SymmetricUtduSolver(mg.UtduSolverOptions(Ordering=ordering, Precision=mg.Precision.FP64))
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        del f
-        if args.fp64_first:
-            e0.record(stream)
-            f64 = f64s.Factorize(m, sym)
-        else:
-            f64 = f64s.Factorize(m, sym)
-            e0.record(stream)
-            f64.RefactorizeDevice(d_vals.data_ptr())
-        f64.SolveDevice(d_b.data_ptr(), d_x.data_ptr(), nrhs)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        s64 = e0.elapsed_time(e1) / 1e3
-        rr64 = worst_relres(f64, d_x.cpu().numpy())
-        fp64 = {"factor_solve_s": s64, "tflops": ops / s64 / 1e12, "relres": float(rr64),
-                "speedup_mixed_vs_fp64": s64 / (ms / 1e3),
-                "timed": "first factorisation + solve" if args.fp64_first else "refactorisation + solve"}
     if rank != 0:
         return
     cb = None if args.no_cpu_baseline else cpu_baseline(args, os.cpu_count() or 1)
     value = world * ops / (ms / 1e3) / 1e12
+    entries = sym.FactorEntryCount
+    apps = [it + 1 for it in iters]   # factor applications per refined solve (x0 plus one per step)
     line = {
         "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": "bf16" if prec == mg.Precision.BF16 else ("tf32" if prec == mg.Precision.TF32 else "f64"),
+        "dtype": {mg.Precision.BF16: "bf16", mg.Precision.TF32: "tf32", mg.Precision.FP64: "f64"}[prec],
         "data": "synthetic",
         "config": {"workload": f"elasticity Q1 {args.elements[0]}x{args.elements[1]}x{args.elements[2]} elements, "
-                               f"n={m.Size}, nnz_upper={m.NonZeroCount}, {args.ordering} ordering",
-                   "precision": f"{prec.name} Schur GEMMs (FP32 accumulation), FP32 fronts and pivot blocks, FP64-residual refinement",
+                               f"n={m.Size}, nnz_upper={m.NonZeroCount}, {args.ordering} ordering, {nrhs} right-hand "
+                               f"sides, {max(1, args.perturbations)} value sets"
+                               + (" (E x (1 + uniform[-0.05, 0.05]) per element)" if args.perturbations else ""),
+                   "precision": (f"{prec.name} Schur GEMMs (FP32 accumulation), FP32 fronts, FP64-residual refinement"
+                                 if prec != mg.Precision.FP64 else "FP64 throughout"),
                    "refine_tol": args.tol, "factor_ops": ops, "parallelism": f"replicas{world}", "nrhs": nrhs,
                    "l2": "inputs larger than L2 (no flush)"},
-        "factor_solve_s": ms / 1e3, "refine_iterations": iters, "relres": float(relres),
+        "factor_solve_s": ms / 1e3, "refine_iterations": iters,
+        "relres": float(max(relres_steps + [relres0])),
+        "forward_error_vs_fp64_gpu": fwd_err,
+        "flops_per_step": {"factor": ops,
+                           "solves": float(sum(apps) / len(apps) * nrhs * (4.0 * (entries - m.Size) + m.Size)),
+                           "refinement_spmv": float(sum(apps) / len(apps) * 2 * nrhs * 4.0 * m.NonZeroCount)},
         "symbolic_s": t_sym,
         "e2e": {"value": world * ops / (e2e / 1e3) / 1e12, "unit": "TFLOP/s", "ms_per_step": e2e,
                 "h2d_bytes_per_step": int(m.NonZeroCount * 8 + m.Size * 8 * nrhs),
                 "d2h_bytes_per_step": int(m.Size * 8 * nrhs),
-                "relres": e2e_relres},
+                "relres": float(max(r for r in e2e_rr if r is not None)) if any(r is not None for r in e2e_rr) else None},
         "gpu_launches": int(launches),
         "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak if peak else None, "traffic": traffic,
                      "kernel": "k_tc_gemm", "launches_per_step": ph["schur_tensor_launches"],
-                     "note": "peak = bf16_tflops_sustained of MEASURED_PEAKS.json (half of it for TF32)"},
+                     "note": "peak = bf16_tflops_sustained of MEASURED_PEAKS.json (half of it for TF32), of measured"},
         "phases_ms": {k: ph[k] for k in ("pivot_block_ms", "panel_ms", "schur_ms", "extend_add_ms", "small_fronts_ms",
                                           "total_ms")},
+        "solve_phases_ms": {**{k: round(v, 3) for k, v in ph["solve_ms"].items()}, "total": ph["solve_total_ms"]},
         "clocks": clocks.summary(),
         "cpu_baseline": cb,
     }
@@ -304,6 +363,14 @@ def run_ours(args):
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+def _with_values(m, values):
+    """A matrix of m's pattern holding the given values."""
+    import copy
+    mk = copy.copy(m)
+    mk._val = np.ascontiguousarray(values, np.float64)
+    return mk
 
 
 def gemm_traffic(args, prec):

@@ -161,6 +161,8 @@ int uchol_solve_refined_device(uchol_factor f, int n, int nrhs, const double* d_
 int uchol_residual_norms(uchol_factor f, int n, int nrhs, const double* b, int ldb, const double* x, int ldx,
                          double* out_norms);
 
+#define UCHOL_SOLVE_KINDS 9
+
 /* Device-time of the last call on the handle's stream, per phase. */
 typedef struct {
     double pivot_block_ms, extend_add_ms, small_fronts_ms, panel_ms, schur_ms, total_ms;  /* filled when UCHOL_PHASE_TIMES is set */
@@ -168,6 +170,14 @@ typedef struct {
     double schur_tensor_flops;   /* algorithmic flops of the tensor-core Schur updates (lower triangle) */
     double schur_tensor_ms;      /* their device time (UCHOL_PHASE_TIMES) */
     int schur_tensor_launches;
+    /* Triangular solves (filled by a solve made while phase timing is on; that solve
+     * launches its kernels directly instead of replaying its graph).  Index: 0 forward
+     * gather, 1 forward single-block fronts, 2 forward level kernels, 3 backward gather,
+     * 4 backward column dots, 5 backward single-block fronts, 6 backward level kernels,
+     * 7 forward trailing rows of single-block fronts, 8 backward partial-sum reductions. */
+    double solve_kind_ms[UCHOL_SOLVE_KINDS];
+    double solve_total_ms;       /* sum over the solve's launches */
+    int solve_launches;
 } uchol_phase_times;
 int uchol_factor_phase_times(uchol_factor f, uchol_phase_times* t);
 

@@ -521,6 +521,30 @@ void factorize_impl(uchol_factor_s* F, const double* values, bool on_device) {
     uchol_symbolic_s* S = F->sym;
     cudaStream_t st = S->stream;
     const Plan& P = F->dp->plan;
+    // the whole launch sequence is captured once per factor and replayed:
+    // refactorisations with the same pattern cost one graph launch.  The capture
+    // (host work) and the graph's upload come before the timed region, so that
+    // factor_ms of a first factorisation equals that of a refactorisation.
+    if (!phase_timing() && !F->factor_graph) {
+        if (!F->capture_stream) CK(cudaStreamCreateWithFlags(&F->capture_stream, cudaStreamNonBlocking));
+        cudaGraph_t g = nullptr;
+        const long long before = g_launches.load();
+        CK(cudaStreamBeginCapture(F->capture_stream, cudaStreamCaptureModeThreadLocal));
+        try {
+            enqueue_factorization(F, F->capture_stream);
+        } catch (...) {
+            cudaStreamEndCapture(F->capture_stream, &g);
+            if (g) cudaGraphDestroy(g);
+            throw;
+        }
+        CK(cudaStreamEndCapture(F->capture_stream, &g));
+        F->factor_graph_nodes = (int)(g_launches.load() - before);
+        g_launches -= F->factor_graph_nodes;   // counted when the graph runs
+        cudaError_t e = cudaGraphInstantiate(&F->factor_graph, g, 0);
+        cudaGraphDestroy(g);
+        CK(e);
+        CK(cudaGraphUpload(F->factor_graph, st));
+    }
     StreamTimer total(st);
     if (on_device)
         CK(cudaMemcpyAsync(F->values.p, values, (size_t)S->nnz * sizeof(double), cudaMemcpyDeviceToDevice, st));
@@ -530,27 +554,6 @@ void factorize_impl(uchol_factor_s* F, const double* values, bool on_device) {
     if (phase_timing()) {
         enqueue_factorization(F, st);   // direct launches, one event pair each
     } else {
-        // the whole launch sequence is captured once per factor and replayed:
-        // refactorisations with the same pattern cost one graph launch
-        if (!F->factor_graph) {
-            if (!F->capture_stream) CK(cudaStreamCreateWithFlags(&F->capture_stream, cudaStreamNonBlocking));
-            cudaGraph_t g = nullptr;
-            const long long before = g_launches.load();
-            CK(cudaStreamBeginCapture(F->capture_stream, cudaStreamCaptureModeThreadLocal));
-            try {
-                enqueue_factorization(F, F->capture_stream);
-            } catch (...) {
-                cudaStreamEndCapture(F->capture_stream, &g);
-                if (g) cudaGraphDestroy(g);
-                throw;
-            }
-            CK(cudaStreamEndCapture(F->capture_stream, &g));
-            F->factor_graph_nodes = (int)(g_launches.load() - before);
-            g_launches -= F->factor_graph_nodes;   // counted when the graph runs
-            cudaError_t e = cudaGraphInstantiate(&F->factor_graph, g, 0);
-            cudaGraphDestroy(g);
-            CK(e);
-        }
         CK(cudaGraphLaunch(F->factor_graph, st));
         counted(F->factor_graph_nodes);
     }
@@ -682,8 +685,42 @@ void check_solve_status(uchol_factor_s* F) {
     }
 }
 
-template <class T, class Cv, int SB>
-void run_solve(uchol_factor_s* F, int nrhs, Cv* work, Cv* fv, Cv* fv2, cudaStream_t st) {
+// RG: right-hand sides the level kernels and the backward column dots carry together.
+// Optional per-launch device timing of a solve (direct launches, one event pair each).
+struct SolveTimer {
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev;
+    std::vector<int> kind;
+    void begin(int k, cudaStream_t st) {
+        cudaEvent_t a, b;
+        CK(cudaEventCreate(&a));
+        CK(cudaEventCreate(&b));
+        CK(cudaEventRecord(a, st));
+        ev.push_back({a, b});
+        kind.push_back(k);
+    }
+    void end(cudaStream_t st) { CK(cudaEventRecord(ev.back().second, st)); }
+    // sums per launch kind into t (after the stream has completed)
+    void collect(uchol_phase_times& t) {
+        for (double& v : t.solve_kind_ms) v = 0.0;
+        t.solve_total_ms = 0.0;
+        t.solve_launches = (int)ev.size();
+        for (size_t q = 0; q < ev.size(); ++q) {
+            float ms = 0.f;
+            CK(cudaEventElapsedTime(&ms, ev[q].first, ev[q].second));
+            if (kind[q] >= 0 && kind[q] < UCHOL_SOLVE_KINDS) t.solve_kind_ms[kind[q]] += ms;
+            t.solve_total_ms += ms;
+        }
+    }
+    ~SolveTimer() {
+        for (auto& e : ev) {
+            cudaEventDestroy(e.first);
+            cudaEventDestroy(e.second);
+        }
+    }
+};
+
+template <class T, class Cv, int SB, int RG>
+void run_solve(uchol_factor_s* F, int nrhs, Cv* work, Cv* fv, Cv* fv2, cudaStream_t st, SolveTimer* timer = nullptr) {
     uchol_symbolic_s* S = F->sym;
     DevPlan& D = *F->dp;
     const Plan& P = D.plan;
@@ -708,7 +745,7 @@ void run_solve(uchol_factor_s* F, int nrhs, Cv* work, Cv* fv, Cv* fv2, cudaStrea
     int* progress = bwd_flags + nblocks;
     int* status = F->solve_status.as<int>();
     CK(cudaMemsetAsync(fwd_flags, 0, sizeof(int) * ((size_t)2 * nblocks + P.progress_count), st));
-    const size_t smem = SB * SB * (sizeof(T) + sizeof(Cv)) + kLevelSmemSlack;
+    const size_t smem = level_smem_bytes<T, Cv, SB, RG>();
     auto level_args = [&](const SolveLaunch& L, int* flags, int grid) {
         LevelArgs la;
         la.chains = tasks + L.begin;
@@ -742,8 +779,9 @@ void run_solve(uchol_factor_s* F, int nrhs, Cv* work, Cv* fv, Cv* fv2, cudaStrea
     };
     for (const SolveLaunch& L : P.fwd_launches) {
         if (L.count == 0) continue;
+        if (timer) timer->begin((int)L.kind, st);
         if (L.kind == SolveLaunch::FwdGather) {
-            k_fwd_gather<Cv><<<L.count, 256, 0, st>>>(tasks + L.begin, A, work, fv);
+            k_fwd_gather<Cv><<<dim3(L.count, std::min(nrhs, 65535)), 256, 0, st>>>(tasks + L.begin, A, work, fv);
         } else if (L.kind == SolveLaunch::FwdSolo) {
             k_fwd_solo<T, Cv, SB><<<L.count, 256, 0, st>>>(tasks + L.begin, A, panel, linv, fv, fv2, diag, work);
         } else if (L.kind == SolveLaunch::FwdTail) {
@@ -753,25 +791,28 @@ void run_solve(uchol_factor_s* F, int nrhs, Cv* work, Cv* fv, Cv* fv2, cudaStrea
                 k_fwd_tail<T, Cv, SB, 4><<<L.count, kTailRows / 4, 0, st>>>(tasks + L.begin, A, panel, fv2, fv);
         } else {
             const int grid = F->coop_fwd;
-            launch_cooperative(k_fwd_level<T, Cv, SB>, grid, 256, smem, st, level_args(L, fwd_flags, grid), A, panel,
+            launch_cooperative(k_fwd_level<T, Cv, SB, RG>, grid, 256, smem, st, level_args(L, fwd_flags, grid), A, panel,
                                linv, fv, fv2, diag, work);
         }
+        if (timer) timer->end(st);
     }
     for (const SolveLaunch& L : P.bwd_launches) {
         if (L.count == 0) continue;
+        if (timer) timer->begin((int)L.kind, st);
         if (L.kind == SolveLaunch::BwdGather) {
-            k_bwd_gather<Cv><<<L.count, 256, 0, st>>>(tasks + L.begin, A, work, fv);
+            k_bwd_gather<Cv><<<dim3(L.count, std::min(nrhs, 65535)), 256, 0, st>>>(tasks + L.begin, A, work, fv);
         } else if (L.kind == SolveLaunch::BwdTail) {
-            k_bwd_cols<T, Cv><<<L.count, 256, 0, st>>>(tasks + L.begin, A, panel, fv, F->bwd_partial.as<Cv>());
+            k_bwd_cols<T, Cv, RG><<<L.count, 256, 0, st>>>(tasks + L.begin, A, panel, fv, F->bwd_partial.as<Cv>());
         } else if (L.kind == SolveLaunch::BwdTailReduce) {
             k_bwd_cols_reduce<Cv><<<L.count, 128, 0, st>>>(tasks + L.begin, A, F->bwd_partial.as<Cv>(), fv);
         } else if (L.kind == SolveLaunch::BwdSolo) {
             k_bwd_solo<Cv, SB><<<L.count, 256, 0, st>>>(tasks + L.begin, A, linv, fv, fv2, work);
         } else {
             const int grid = F->coop_bwd;
-            launch_cooperative(k_bwd_level<T, Cv, SB>, grid, 256, smem, st, level_args(L, bwd_flags, grid), A, panel,
+            launch_cooperative(k_bwd_level<T, Cv, SB, RG>, grid, 256, smem, st, level_args(L, bwd_flags, grid), A, panel,
                                linv, fv, fv2, work);
         }
+        if (timer) timer->end(st);
     }
     CK(cudaGetLastError());
 }
@@ -796,14 +837,20 @@ void launch_solve_graph(uchol_factor_s* F, int nrhs, Cv* work, cudaStream_t st) 
         }
         if (!F->capture_stream) CK(cudaStreamCreateWithFlags(&F->capture_stream, cudaStreamNonBlocking));
         // the level kernels run as cooperative launches: at most as many CTAs as the device holds at once
-        const int smem = (int)(SB * SB * (sizeof(T) + sizeof(Cv)) + kLevelSmemSlack);
-        CK(cudaFuncSetAttribute(k_fwd_level<T, Cv, SB>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-        CK(cudaFuncSetAttribute(k_bwd_level<T, Cv, SB>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-        int per_sm = 0;
-        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fwd_level<T, Cv, SB>, 256, smem));
-        F->coop_fwd = per_sm * F->sms;
-        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bwd_level<T, Cv, SB>, 256, smem));
-        F->coop_bwd = per_sm * F->sms;
+        auto level_kernels = [&](auto* fwd, auto* bwd, int smem) {
+            CK(cudaFuncSetAttribute(fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+            CK(cudaFuncSetAttribute(bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+            int per_sm = 0;
+            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fwd, 256, smem));
+            F->coop_fwd = per_sm * F->sms;
+            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bwd, 256, smem));
+            F->coop_bwd = per_sm * F->sms;
+        };
+        if (nrhs == 1)
+            level_kernels(k_fwd_level<T, Cv, SB, 1>, k_bwd_level<T, Cv, SB, 1>, (int)level_smem_bytes<T, Cv, SB, 1>());
+        else
+            level_kernels(k_fwd_level<T, Cv, SB, kSolveRhsGroup>, k_bwd_level<T, Cv, SB, kSolveRhsGroup>,
+                          (int)level_smem_bytes<T, Cv, SB, kSolveRhsGroup>());
         if (F->coop_fwd < 2 || F->coop_bwd < 2) throw Error(UCHOL_CUDA_ERROR, "the level solve kernels do not fit");
         if (!F->solve_maps.p) {
             // tile copies of the level solves: each front's panel (m x w)
@@ -837,7 +884,10 @@ void launch_solve_graph(uchol_factor_s* F, int nrhs, Cv* work, cudaStream_t st) 
         cudaGraph_t g = nullptr;
         CK(cudaStreamBeginCapture(F->capture_stream, cudaStreamCaptureModeThreadLocal));
         try {
-            run_solve<T, Cv, SB>(F, nrhs, work, F->fv.as<Cv>(), F->fv2.as<Cv>(), F->capture_stream);
+            if (nrhs == 1)
+                run_solve<T, Cv, SB, 1>(F, nrhs, work, F->fv.as<Cv>(), F->fv2.as<Cv>(), F->capture_stream);
+            else
+                run_solve<T, Cv, SB, kSolveRhsGroup>(F, nrhs, work, F->fv.as<Cv>(), F->fv2.as<Cv>(), F->capture_stream);
         } catch (...) {
             cudaStreamEndCapture(F->capture_stream, &g);
             if (g) cudaGraphDestroy(g);
@@ -849,6 +899,18 @@ void launch_solve_graph(uchol_factor_s* F, int nrhs, Cv* work, cudaStream_t st) 
         CK(e);
         F->solve_graph_nrhs = nrhs;
         F->solve_graph_nodes = solve_launch_count(F->dp->plan);
+    }
+    if (phase_timing()) {
+        // direct launches with one event pair each (the graph above stays for untimed calls)
+        SolveTimer timer;
+        if (nrhs == 1)
+            run_solve<T, Cv, SB, 1>(F, nrhs, work, F->fv.as<Cv>(), F->fv2.as<Cv>(), st, &timer);
+        else
+            run_solve<T, Cv, SB, kSolveRhsGroup>(F, nrhs, work, F->fv.as<Cv>(), F->fv2.as<Cv>(), st, &timer);
+        CK(cudaStreamSynchronize(st));
+        timer.collect(F->phases);
+        counted(F->solve_graph_nodes);
+        return;
     }
     CK(cudaGraphLaunch(F->solve_graph, st));
     counted(F->solve_graph_nodes);

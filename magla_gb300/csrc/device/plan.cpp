@@ -442,7 +442,7 @@ Plan build_from_fronts(int n, int count, const int* first_column, const int* par
         for (int k0 = 0; k0 < P.sn[s].w; k0 += SB)
             P.inv_blocks.push_back({s, k0, std::min(SB, P.sn[s].w - k0), 0, 0, 1, (int)P.inv_blocks.size()});
     }
-    constexpr int kGatherChunk = 2048;
+    constexpr int kGatherChunk = 512;   // rows per gather CTA (one CTA per chunk and right-hand side)
     // chunked per-front tasks: rows [r0, r1) of the front vector
     auto gather_tasks = [&](const std::vector<int>& fronts) {
         int b = (int)P.solve_tasks.size();

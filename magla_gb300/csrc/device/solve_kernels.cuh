@@ -80,7 +80,8 @@ __global__ void k_fwd_gather(const SolveBlockTask* __restrict__ tasks, SolveArgs
     const int s = tk.s;
     const SnDev d = A.sn[s];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int r = 0; r < A.nrhs; ++r) {
+    // right-hand sides blockIdx.y, blockIdx.y + gridDim.y, ...
+    for (int r = blockIdx.y; r < A.nrhs; r += gridDim.y) {
         Cv* f = fv + A.fvec_off[s] + r * A.fv_stride;
         for (int a = tk.r0 + threadIdx.x; a < tk.r1; a += blockDim.x)
             f[a] = a < d.w ? work[d.first_col + a + (long long)r * A.ldw] : Cv(0);
@@ -102,7 +103,7 @@ __global__ void k_fwd_gather(const SolveBlockTask* __restrict__ tasks, SolveArgs
             if (lane == 0) range[warp] = v;
         }
         __syncthreads();
-        for (int r = 0; r < A.nrhs; ++r) {
+        for (int r = blockIdx.y; r < A.nrhs; r += gridDim.y) {
             Cv* f = fv + A.fvec_off[s] + r * A.fv_stride;
             const Cv* u = fv + A.fvec_off[ch] + r * A.fv_stride + cd.w;
             for (int b = range[0] + threadIdx.x; b < range[1]; b += blockDim.x) f[rl[b]] += u[b];
@@ -165,6 +166,7 @@ __global__ void __launch_bounds__(SB) k_invert_blocks(const SolveBlockTask* __re
 
 constexpr unsigned long long kSolveWaitNs = 1000000000ull;   // 1 s per bounded wait
 constexpr size_t kLevelSmemSlack = 1024;                      // alignment slack of the level kernels' dynamic smem
+constexpr int kSolveRhsGroup = 16;                            // right-hand sides per group of the multi-column solves
 constexpr int kSolveStatusTimeout = 2;
 
 __device__ __forceinline__ unsigned long long solve_ns() {
@@ -346,30 +348,117 @@ __device__ __forceinline__ bool next_chain_duty(const LevelArgs& L, int& q, int&
     }
 }
 
+// Right-hand sides of the level kernels.  RG columns of the solve go through
+// each chain duty and each bulk item together: the current solution block
+// (y or x) and the solved block's right-hand side (f or g) sit in shared memory
+// as SB rows of RG values (row stride RS, padded so that the backward kernel's
+// skewed rows are read without bank conflicts), next to the partial sums of the
+// TP thread groups that split each product.
+template <class Cv, int SB, int RG>
+struct LevelRhs {
+    static constexpr int TP = 256 / SB;                  // thread groups splitting one product
+    static constexpr int RS = RG >= 4 ? RG + 4 : RG;     // row stride of the solution and right-hand blocks
+    static constexpr int FG = RG >= TP ? RG / TP : RG;   // right-hand sides one thread finishes
+    static constexpr size_t bytes = (size_t)(2 * SB * RS + TP * SB * RG) * sizeof(Cv);
+};
+
+// Dynamic shared memory of a level kernel: two tile buffers, then the right-hand-side area.
+template <class T, class Cv, int SB, int RG>
+constexpr size_t level_smem_bytes() {
+    return (size_t)SB * SB * (sizeof(T) + sizeof(Cv)) + LevelRhs<Cv, SB, RG>::bytes + kLevelSmemSlack;
+}
+
+// Sums of RG right-hand sides.  With one right-hand side four independent sums
+// hide the latency of the multiply-adds; with several, the right-hand sides do.
+template <class Cv, int RG>
+struct RhsAcc {
+    static constexpr int NA = RG >= 4 ? 1 : 4;
+    Cv v[NA][RG];
+    __device__ __forceinline__ void zero() {
+#pragma unroll
+        for (int a = 0; a < NA; ++a)
+#pragma unroll
+            for (int g = 0; g < RG; ++g) v[a][g] = Cv(0);
+    }
+    // v[j] += t * y[0, RG) (y: 16-byte aligned when RG is a multiple of 4); j is a compile-time index
+    __device__ __forceinline__ void add(int j, Cv t, const Cv* y) {
+        Cv* a = v[j & (NA - 1)];
+        if constexpr (RG % 4 == 0 && sizeof(Cv) == 4) {
+#pragma unroll
+            for (int g = 0; g < RG; g += 4) {
+                const float4 q = *reinterpret_cast<const float4*>(y + g);
+                a[g] += t * q.x;
+                a[g + 1] += t * q.y;
+                a[g + 2] += t * q.z;
+                a[g + 3] += t * q.w;
+            }
+        } else if constexpr (RG % 2 == 0 && sizeof(Cv) == 8) {
+#pragma unroll
+            for (int g = 0; g < RG; g += 2) {
+                const double2 q = *reinterpret_cast<const double2*>(y + g);
+                a[g] += t * q.x;
+                a[g + 1] += t * q.y;
+            }
+        } else {
+#pragma unroll
+            for (int g = 0; g < RG; ++g) a[g] += t * y[g];
+        }
+    }
+    __device__ __forceinline__ Cv sum(int g) const {
+        if constexpr (NA == 4) return (v[0][g] + v[1][g]) + (v[2][g] + v[3][g]);
+        else return v[0][g];
+    }
+    // p[0, RG) = the sums (16-byte aligned when RG is a multiple of 4)
+    __device__ __forceinline__ void store(Cv* p) const {
+        if constexpr (RG % 4 == 0 && sizeof(Cv) == 4) {
+#pragma unroll
+            for (int g = 0; g < RG; g += 4)
+                *reinterpret_cast<float4*>(p + g) = make_float4(sum(g), sum(g + 1), sum(g + 2), sum(g + 3));
+        } else {
+#pragma unroll
+            for (int g = 0; g < RG; ++g) p[g] = sum(g);
+        }
+    }
+};
+
 // Forward.  Chain duty (front, b): y_{b+1} = L_{b+1}^-1 (f_{b+1} - L[b+1, b] y_b),
 // where the bulk has already applied y_0 .. y_{b-1} to f_{b+1}; writes y and
 // y / D (the work vector).  Bulk chunk of diagonal block `own` applies
 // y_0 .. y_{own-2}; a chunk of trailing rows applies every y_b and ends as
 // the front's update vector.  Both sides: SB rows, 256 / SB threads per row
-// splitting the columns.
-template <class T, class Cv, int SB>
+// splitting the columns, RG right-hand sides at a time.
+template <class T, class Cv, int SB, int RG>
 __global__ void __launch_bounds__(256, 1) k_fwd_level(LevelArgs L, SolveArgs A, const T* __restrict__ panel,
                                                       const Cv* __restrict__ linv, Cv* fv, Cv* yv,
                                                       const double* __restrict__ diag, Cv* work) {
-    constexpr int TPR = 256 / SB;   // threads per row
-    constexpr int CPT = SB / TPR;   // columns per thread
+    using R = LevelRhs<Cv, SB, RG>;
+    constexpr int TPR = R::TP;       // threads per row
+    constexpr int CPT = SB / TPR;    // columns per thread
+    constexpr int RS = R::RS, FG = R::FG;
     extern __shared__ __align__(128) unsigned char blk_smem[];
     // copy destinations aligned to 1024 bytes (the launch adds kLevelSmemSlack)
     unsigned char* sm = blk_smem + ((1024u - (smem_addr(blk_smem) & 1023u)) & 1023u);
     T* Tl = reinterpret_cast<T*>(sm);                          // tile L[b+1, b], column-major
     Cv* Li = reinterpret_cast<Cv*>(sm + SB * SB * sizeof(T));  // inverse of block b+1, column-major
-    __shared__ Cv yb[SB];
-    __shared__ Cv fb[SB];
-    __shared__ Cv part[256];
+    Cv* yb = Li + SB * SB;                                     // y_b: SB rows x RG
+    Cv* fb = yb + SB * RS;                                     // f_{b+1} - L[b+1, b] y_b
+    Cv* part = fb + SB * RS;                                   // [TPR][SB][RG] partial sums
     __shared__ int ok;
     __shared__ unsigned long long tbar;
     __shared__ unsigned long long sbar[2];
     const int tid = threadIdx.x, row = tid % SB, pid = tid / SB;
+    // the thread finishing right-hand sides [g0, g0 + FG) of its row
+    const bool fin = RG >= TPR || pid == 0;
+    const int g0 = RG >= TPR ? pid * FG : 0;
+    const int nr = A.nrhs;
+    const bool one_group = nr <= RG;
+    // y_b of right-hand sides [rg, rg + ng) into yb (zero past kb rows and ng columns)
+    auto load_y = [&](long long fo, int rg, int ng, int b, int kb) {
+        for (int t = tid; t < SB * RG; t += blockDim.x) {
+            const int g = t / SB, k = t - g * SB;
+            yb[k * RS + g] = (g < ng && k < kb) ? __ldcg(yv + fo + (long long)(rg + g) * A.fv_stride + b * SB + k) : Cv(0);
+        }
+    };
     if ((int)blockIdx.x < L.nchain_cta) {
         // tile rows past a partial block are multiplied by zero: start from zeros, not stale bits
         for (int i = tid; i < SB * SB; i += blockDim.x) {
@@ -399,63 +488,86 @@ __global__ void __launch_bounds__(256, 1) k_fwd_level(LevelArgs L, SolveArgs A, 
                                        linv + (long long)(c.blk + bb + 1) * SB * SB, kn, &tbar);
         };
         prefetch(q, b);
-        int held = -1;   // front whose y_b is in yb (single right-hand side)
+        int held = -1;   // front whose y_b is in yb (all right-hand sides in one group)
         for (;;) {
             front(q);
             const int r0 = (b + 1) * SB, kn = min(SB, d.w - r0);
-            for (int r = 0; r < A.nrhs; ++r) {
-                const long long base = A.fvec_off[c.s] + r * A.fv_stride;
-                if (b >= 0 && !(A.nrhs == 1 && held == q)) {
+            const int kb = b >= 0 ? min(SB, d.w - b * SB) : 0;
+            const long long fo = A.fvec_off[c.s];
+            for (int rg = 0; rg < nr; rg += RG) {
+                const int ng = min(RG, nr - rg);
+                if (b >= 0 && !(one_group && held == q)) {
                     __syncthreads();
-                    for (int t = tid; t < SB; t += blockDim.x) yb[t] = __ldcg(yv + base + b * SB + t);
+                    load_y(fo, rg, ng, b, kb);
                 }
-                if (r == 0) {
+                if (rg == 0) {
                     if (!__syncthreads_and(bar_wait(&tbar, phase, L.status))) return;
                     phase ^= 1;
                 }
                 __syncthreads();
                 // f_{b+1} - L[b+1, b] y_b: thread (row, pid) sums columns [pid CPT, pid CPT + CPT)
-                Cv a4[4] = {Cv(0), Cv(0), Cv(0), Cv(0)};
+                RhsAcc<Cv, RG> acc;
+                acc.zero();
                 if (b >= 0) {
-#pragma unroll 8
-                    for (int u = 0; u < CPT; ++u) a4[u & 3] += (Cv)Tl[row + (pid * CPT + u) * SB] * yb[pid * CPT + u];
+#pragma unroll 2
+                    for (int u0 = 0; u0 < CPT; u0 += 4)
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) {
+                            const int k = pid * CPT + u0 + j;
+                            acc.add(j, (Cv)Tl[row + k * SB], yb + k * RS);
+                        }
                 }
-                part[tid] = (a4[0] + a4[1]) + (a4[2] + a4[3]);
+                acc.store(part + (pid * SB + row) * RG);
                 // only now the bulk's part: chunk b+1 has applied y_0 .. y_{b-1} (the product above
                 // needs neither it nor f, so it overlaps the bulk's last update)
-                if (r == 0 && b >= 1 && !wait_at_least(L.progress + c.k0 + b + 1, b, L.status, &ok)) return;
-                const Cv f0 = (pid == 0 && row < kn) ? __ldcg(fv + base + r0 + row) : Cv(0);
-                __syncthreads();
-                if (pid == 0) {
-                    Cv v = f0;
+                if (rg == 0 && b >= 1 && !wait_at_least(L.progress + c.k0 + b + 1, b, L.status, &ok)) return;
+                Cv f0[FG];
 #pragma unroll
-                    for (int p = 0; p < TPR; ++p) v -= part[row + p * SB];
-                    fb[row] = row < kn ? v : Cv(0);
+                for (int j = 0; j < FG; ++j) {
+                    const int g = g0 + j;
+                    f0[j] = (fin && row < kn && g < ng) ? __ldcg(fv + fo + (long long)(rg + g) * A.fv_stride + r0 + row)
+                                                        : Cv(0);
+                }
+                __syncthreads();
+                if (fin) {
+#pragma unroll
+                    for (int j = 0; j < FG; ++j) {
+                        const int g = g0 + j;
+                        Cv v = f0[j];
+#pragma unroll
+                        for (int p = 0; p < TPR; ++p) v -= part[(p * SB + row) * RG + g];
+                        fb[row * RS + g] = row < kn ? v : Cv(0);
+                    }
                 }
                 __syncthreads();
                 // y = L_{b+1}^-1 f: thread (row, pid) sums k in [pid CPT, pid CPT + CPT), k <= row
-                Cv s0 = Cv(0), s1 = Cv(0), s2 = Cv(0), s3 = Cv(0);
-                const int kend = min(pid * CPT + CPT, row + 1);
-                int k = pid * CPT;
-                for (; k + 4 <= kend; k += 4) {
-                    s0 += Li[row + k * SB] * fb[k];
-                    s1 += Li[row + (k + 1) * SB] * fb[k + 1];
-                    s2 += Li[row + (k + 2) * SB] * fb[k + 2];
-                    s3 += Li[row + (k + 3) * SB] * fb[k + 3];
-                }
-                for (; k < kend; ++k) s0 += Li[row + k * SB] * fb[k];
-                part[tid] = (s0 + s1) + (s2 + s3);
-                __syncthreads();
-                if (pid == 0 && row < kn) {
-                    Cv y = part[row];
+                acc.zero();
+                {
+                    const int kend = min(pid * CPT + CPT, row + 1);
+                    int k = pid * CPT;
+                    for (; k + 4 <= kend; k += 4)
 #pragma unroll
-                    for (int p = 1; p < TPR; ++p) y += part[row + p * SB];
-                    const int col = r0 + row;
-                    yv[base + col] = y;
-                    yb[row] = y;   // y_{b+1}, kept for this front's next duty
-                    work[d.first_col + col + (long long)r * A.ldw] = (Cv)((double)y / diag[d.first_col + col]);
-                } else if (pid == 0) {
-                    yb[row] = Cv(0);
+                        for (int j = 0; j < 4; ++j) acc.add(j, Li[row + (k + j) * SB], fb + (k + j) * RS);
+                    for (; k < kend; ++k) acc.add(0, Li[row + k * SB], fb + k * RS);
+                }
+                acc.store(part + (pid * SB + row) * RG);
+                __syncthreads();
+                if (fin) {
+#pragma unroll
+                    for (int j = 0; j < FG; ++j) {
+                        const int g = g0 + j;
+                        Cv y = part[row * RG + g];
+#pragma unroll
+                        for (int p = 1; p < TPR; ++p) y += part[(p * SB + row) * RG + g];
+                        const bool live = row < kn && g < ng;
+                        if (live) {
+                            const int col = r0 + row;
+                            yv[fo + (long long)(rg + g) * A.fv_stride + col] = y;
+                            work[d.first_col + col + (long long)(rg + g) * A.ldw] =
+                                (Cv)((double)y / diag[d.first_col + col]);
+                        }
+                        yb[row * RS + g] = live ? y : Cv(0);   // y_{b+1}, kept for this front's next duty
+                    }
                 }
             }
             held = q;
@@ -468,8 +580,8 @@ __global__ void __launch_bounds__(256, 1) k_fwd_level(LevelArgs L, SolveArgs A, 
     // Tiles come by tensor-map copies into two stage buffers (the chain's tile and inverse space),
     // the next item's copy in flight while the current one is applied; the flag and y_b of
     // consecutive items of one front are shared.
-    const BulkRange R = bulk_range(L);
-    if (R.begin >= R.end || R.step <= 0) return;
+    const BulkRange Rg = bulk_range(L);
+    if (Rg.begin >= Rg.end || Rg.step <= 0) return;
     auto stage = [&](int k) { return k ? reinterpret_cast<T*>(Li) : Tl; };
     if (tid == 0) {
         bar_init(&sbar[0]);
@@ -479,8 +591,8 @@ __global__ void __launch_bounds__(256, 1) k_fwd_level(LevelArgs L, SolveArgs A, 
     unsigned phbits = 0;   // expected parity of each stage barrier
     auto next_item = [&](int& b, int& q) {
         for (;;) {
-            q = q < 0 ? R.begin : q + R.step;
-            if (q >= R.end) {
+            q = q < 0 ? Rg.begin : q + Rg.step;
+            if (q >= Rg.end) {
                 q = -1;
                 if (++b >= L.steps) return false;
                 continue;
@@ -496,7 +608,9 @@ __global__ void __launch_bounds__(256, 1) k_fwd_level(LevelArgs L, SolveArgs A, 
             start_bulk_tile<T, SB>(stage(st_), L.maps + L.bulk[q].s, L.bulk[q].r0 & ~(kAlign - 1), b * SB, &sbar[st_]);
     };
     int seen_blk = -1, seen_b = -1, prev_q = -1;
-    Cv fcur = Cv(0);   // f of this thread's row of the previous item (single right-hand side)
+    Cv fcur[FG];   // f of this thread's row after the previous item (all right-hand sides in one group)
+#pragma unroll
+    for (int j = 0; j < FG; ++j) fcur[j] = Cv(0);
     int b0 = 0, q0 = -1;
     if (!next_item(b0, q0)) return;
     int b1 = b0, q1 = q0;
@@ -509,35 +623,54 @@ __global__ void __launch_bounds__(256, 1) k_fwd_level(LevelArgs L, SolveArgs A, 
         const SnDev d = A.sn[c.s];
         const int kb = min(SB, d.w - b0 * SB), i = c.r0 + row;
         const bool same = c.blk == seen_blk && b0 == seen_b;
+        const long long fo = A.fvec_off[c.s];
         // f of the row, issued before the waits (this thread wrote it last, if anyone did)
-        Cv fold = Cv(0);
-        if (A.nrhs == 1 && pid == 0 && i < c.r1) fold = q0 == prev_q ? fcur : fv[A.fvec_off[c.s] + i];
+        Cv fold[FG];
+#pragma unroll
+        for (int j = 0; j < FG; ++j) {
+            const int g = g0 + j;
+            fold[j] = (one_group && fin && i < c.r1 && g < nr)
+                          ? (q0 == prev_q ? fcur[j] : fv[fo + (long long)g * A.fv_stride + i])
+                          : Cv(0);
+        }
         if (!same && !wait_at_least(L.flags + c.blk + b0, 1, L.status, &ok)) return;
-        for (int r = 0; r < A.nrhs; ++r) {
-            const long long base = A.fvec_off[c.s] + r * A.fv_stride;
-            if (!(same && A.nrhs == 1)) {
+        for (int rg = 0; rg < nr; rg += RG) {
+            const int ng = min(RG, nr - rg);
+            if (!(same && one_group)) {
                 __syncthreads();
-                for (int t = tid; t < SB; t += blockDim.x) yb[t] = t < kb ? __ldcg(yv + base + b0 * SB + t) : Cv(0);
+                load_y(fo, rg, ng, b0, kb);
             }
-            if (r == 0) {
+            if (rg == 0) {
                 if (!__syncthreads_and(bar_wait(&sbar[cur], (phbits >> cur) & 1u, L.status))) return;
                 phbits ^= 1u << cur;
             }
             __syncthreads();
             const T* tile = stage(cur);
             const int trow = min(row + (c.r0 & (kAlign - 1)), SB - 1);   // idle rows past the chunk: clamped
-            Cv a4[4] = {Cv(0), Cv(0), Cv(0), Cv(0)};
-#pragma unroll 8
-            for (int u = 0; u < CPT; ++u) a4[u & 3] += (Cv)tile[trow + (pid * CPT + u) * SB] * yb[pid * CPT + u];
-            part[tid] = (a4[0] + a4[1]) + (a4[2] + a4[3]);
-            __syncthreads();
-            if (pid == 0 && i < c.r1) {
-                Cv sum = part[row];
+            RhsAcc<Cv, RG> acc;
+            acc.zero();
+#pragma unroll 2
+            for (int u0 = 0; u0 < CPT; u0 += 4)
 #pragma unroll
-                for (int p = 1; p < TPR; ++p) sum += part[row + p * SB];
-                const Cv f = (A.nrhs == 1 ? fold : fv[base + i]) - sum;
-                fv[base + i] = f;
-                fcur = f;
+                for (int j = 0; j < 4; ++j) {
+                    const int k = pid * CPT + u0 + j;
+                    acc.add(j, (Cv)tile[trow + k * SB], yb + k * RS);
+                }
+            acc.store(part + (pid * SB + row) * RG);
+            __syncthreads();
+            if (fin && i < c.r1) {
+#pragma unroll
+                for (int j = 0; j < FG; ++j) {
+                    const int g = g0 + j;
+                    if (g >= ng) break;
+                    Cv sum = part[row * RG + g];
+#pragma unroll
+                    for (int p = 1; p < TPR; ++p) sum += part[(p * SB + row) * RG + g];
+                    Cv* fp = fv + fo + (long long)(rg + g) * A.fv_stride + i;
+                    const Cv f = (one_group ? fold[j] : *fp) - sum;
+                    *fp = f;
+                    fcur[j] = f;
+                }
             }
         }
         seen_blk = c.blk;
@@ -562,25 +695,48 @@ __global__ void __launch_bounds__(256, 1) k_fwd_level(LevelArgs L, SolveArgs A, 
 // L_{b-1}^-T (g_{b-1} - L[b, b-1]^T x_b), where the bulk has already applied
 // x_{nblk-1} .. x_{b+1} to g_{b-1} (t = -1 solves the last block from g after
 // the trailing rows' contribution); writes x to the work vector.  Bulk chunk
-// of own columns of block `own` applies x_{nblk-1} .. x_{own+2}
-// (warp-cooperative dots: warp w takes columns 4w + 32p + (0..3), lanes run
-// over the rows of block b).
-template <class T, class Cv, int SB>
+// of own columns of block `own` applies x_{nblk-1} .. x_{own+2}.  Both sides:
+// thread (column, part) sums its part of the rows in skewed order (row
+// part*RPT + (u + column) mod RPT), so that the threads of a warp read
+// different banks of the column-major tile; RG right-hand sides at a time.
+template <class T, class Cv, int SB, int RG>
 __global__ void __launch_bounds__(256, 1) k_bwd_level(LevelArgs L, SolveArgs A, const T* __restrict__ panel,
                                                       const Cv* __restrict__ linv, Cv* fv, Cv* xv, Cv* work) {
+    using R = LevelRhs<Cv, SB, RG>;
+    constexpr int TPC = R::TP;      // threads per column
+    constexpr int RPT = SB / TPC;   // rows per thread (a power of two)
+    constexpr int RS = R::RS, FG = R::FG;
     extern __shared__ __align__(128) unsigned char blk_smem[];
     unsigned char* sm = blk_smem + ((1024u - (smem_addr(blk_smem) & 1023u)) & 1023u);
     T* Tl = reinterpret_cast<T*>(sm);                          // tile L[b, b-1], column-major
     Cv* Li = reinterpret_cast<Cv*>(sm + SB * SB * sizeof(T));  // inverse of block b-1, column-major
-    __shared__ Cv xb[SB];
-    __shared__ Cv gb[SB];
-    __shared__ Cv part[256];
+    Cv* xb = Li + SB * SB;                                     // x_b: SB rows x RG
+    Cv* gb = xb + SB * RS;                                     // g_{b-1} - L[b, b-1]^T x_b
+    Cv* part = gb + SB * RS;                                   // [TPC][SB][RG] partial sums
     __shared__ int ok;
     __shared__ unsigned long long tbar;
     __shared__ unsigned long long sbar[2];
-    constexpr int TPC = 256 / SB;   // threads per column
-    constexpr int RPT = SB / TPC;   // rows per thread (a power of two)
     const int tid = threadIdx.x, ccol = tid % SB, cpart = tid / SB;
+    const bool fin = RG >= TPC || cpart == 0;
+    const int g0 = RG >= TPC ? cpart * FG : 0;
+    const int nr = A.nrhs;
+    const bool one_group = nr <= RG;
+    auto load_x = [&](long long fo, int rg, int ng, int b, int kb) {
+        for (int e = tid; e < SB * RG; e += blockDim.x) {
+            const int g = e / SB, i = e - g * SB;
+            xb[i * RS + g] = (g < ng && i < kb) ? __ldcg(xv + fo + (long long)(rg + g) * A.fv_stride + b * SB + i) : Cv(0);
+        }
+    };
+    // acc += tile^T x over this thread's rows of column ccol (skewed order)
+    auto tile_t_x = [&](RhsAcc<Cv, RG>& acc, const T* tile) {
+#pragma unroll 2
+        for (int u0 = 0; u0 < RPT; u0 += 4)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int i = cpart * RPT + ((u0 + j + ccol) & (RPT - 1));
+                acc.add(j, (Cv)tile[i + ccol * SB], xb + i * RS);
+            }
+    };
     if ((int)blockIdx.x < L.nchain_cta) {
         // tile rows past a partial block are multiplied by zero: start from zeros, not stale bits
         for (int i = tid; i < SB * SB; i += blockDim.x) {
@@ -609,69 +765,74 @@ __global__ void __launch_bounds__(256, 1) k_bwd_level(LevelArgs L, SolveArgs A, 
                                        linv + (long long)(c.blk + bb - 1) * SB * SB, min(SB, d.w - (bb - 1) * SB), &tbar);
         };
         prefetch(q, t);
-        int held = -1;   // front whose x_b is in xb (single right-hand side)
+        int held = -1;   // front whose x_b is in xb (all right-hand sides in one group)
         for (;;) {
             front(q);
             const int b = c.kn - 1 - t;                        // x_b is applied (t >= 0)
             const int tgt = b - 1;                             // block solved by this duty
             const int c0 = tgt * SB, kn = min(SB, d.w - c0);
             const int kb = t >= 0 ? min(SB, d.w - b * SB) : 0;  // rows of block b
-            for (int r = 0; r < A.nrhs; ++r) {
-                const long long base = A.fvec_off[c.s] + r * A.fv_stride;
-                if (t >= 0 && !(A.nrhs == 1 && held == q)) {
+            const long long fo = A.fvec_off[c.s];
+            for (int rg = 0; rg < nr; rg += RG) {
+                const int ng = min(RG, nr - rg);
+                if (t >= 0 && !(one_group && held == q)) {
                     __syncthreads();
-                    for (int i = tid; i < SB; i += blockDim.x) xb[i] = i < kb ? __ldcg(xv + base + b * SB + i) : Cv(0);
+                    load_x(fo, rg, ng, b, kb);
                 }
-                if (r == 0) {
+                if (rg == 0) {
                     if (!__syncthreads_and(bar_wait(&tbar, phase, L.status))) return;
                     phase ^= 1;
                 }
                 __syncthreads();
-                // g_{b-1} -= L[b, b-1]^T x_b: thread (column, part) sums its part of the rows in
-                // skewed order (row part*RPT + (u + column) mod RPT), so that the threads of a warp
-                // read different banks of the column-major tile
-                if (t >= 0) {
-                    Cv acc = Cv(0);
-#pragma unroll 8
-                    for (int u = 0; u < RPT; ++u) {
-                        const int i = cpart * RPT + ((u + ccol) & (RPT - 1));
-                        acc += (Cv)Tl[i + ccol * SB] * xb[i];
-                    }
-                    part[tid] = acc;
-                }
+                // g_{b-1} -= L[b, b-1]^T x_b
+                RhsAcc<Cv, RG> acc;
+                acc.zero();
+                if (t >= 0) tile_t_x(acc, Tl);
+                acc.store(part + (cpart * SB + ccol) * RG);
                 // only now the bulk's part: chunk b-1 has applied x_{nblk-1} .. x_{b+1}; then g of
-                // the block's columns, one load per thread
-                if (r == 0 && t >= 1 && !wait_at_least(L.progress + c.k0 + tgt, t, L.status, &ok)) return;
-                for (int i = tid; i < kn; i += blockDim.x) gb[i] = __ldcg(fv + base + c0 + i);
-                __syncthreads();
-                if (t >= 0 && cpart == 0 && ccol < kn) {
-                    Cv sum = part[ccol];
-#pragma unroll
-                    for (int p = 1; p < TPC; ++p) sum += part[ccol + p * SB];
-                    gb[ccol] -= sum;
+                // the block's columns
+                if (rg == 0 && t >= 1 && !wait_at_least(L.progress + c.k0 + tgt, t, L.status, &ok)) return;
+                for (int e = tid; e < SB * RG; e += blockDim.x) {
+                    const int g = e / SB, k = e - g * SB;
+                    gb[k * RS + g] = (g < ng && k < kn) ? __ldcg(fv + fo + (long long)(rg + g) * A.fv_stride + c0 + k) : Cv(0);
                 }
                 __syncthreads();
-                // x = Li^T g: column tt of the inverse against g, the same skewed split (k >= tt)
-                {
-                    Cv acc = Cv(0);
-#pragma unroll 8
-                    for (int u = 0; u < RPT; ++u) {
-                        const int k = cpart * RPT + ((u + ccol) & (RPT - 1));
-                        if (k >= ccol && k < kn) acc += Li[k + ccol * SB] * gb[k];
+                if (t >= 0 && fin && ccol < kn) {
+#pragma unroll
+                    for (int j = 0; j < FG; ++j) {
+                        const int g = g0 + j;
+                        Cv sum = part[ccol * RG + g];
+#pragma unroll
+                        for (int p = 1; p < TPC; ++p) sum += part[(p * SB + ccol) * RG + g];
+                        gb[ccol * RS + g] -= sum;
                     }
-                    part[tid] = acc;
                 }
                 __syncthreads();
-                if (cpart == 0) {
-                    Cv x = Cv(0);
-                    if (ccol < kn) {
-                        x = part[ccol];
+                // x = Li^T g: column ccol of the inverse against g, the same skewed split (k >= ccol)
+                acc.zero();
+#pragma unroll 2
+                for (int u0 = 0; u0 < RPT; u0 += 4)
 #pragma unroll
-                        for (int p = 1; p < TPC; ++p) x += part[ccol + p * SB];
-                        xv[base + c0 + ccol] = x;
-                        work[d.first_col + c0 + ccol + (long long)r * A.ldw] = x;
+                    for (int j = 0; j < 4; ++j) {
+                        const int k = cpart * RPT + ((u0 + j + ccol) & (RPT - 1));
+                        if (k >= ccol && k < kn) acc.add(j, Li[k + ccol * SB], gb + k * RS);
                     }
-                    xb[ccol] = x;   // x_{b-1}, kept for this front's next duty (zero past a partial block)
+                acc.store(part + (cpart * SB + ccol) * RG);
+                __syncthreads();
+                if (fin) {
+#pragma unroll
+                    for (int j = 0; j < FG; ++j) {
+                        const int g = g0 + j;
+                        Cv x = part[ccol * RG + g];
+#pragma unroll
+                        for (int p = 1; p < TPC; ++p) x += part[(p * SB + ccol) * RG + g];
+                        const bool live = ccol < kn && g < ng;
+                        if (live) {
+                            xv[fo + (long long)(rg + g) * A.fv_stride + c0 + ccol] = x;
+                            work[d.first_col + c0 + ccol + (long long)(rg + g) * A.ldw] = x;
+                        }
+                        xb[ccol * RS + g] = live ? x : Cv(0);   // x_{b-1}, kept for this front's next duty
+                    }
                 }
             }
             held = q;
@@ -682,8 +843,8 @@ __global__ void __launch_bounds__(256, 1) k_bwd_level(LevelArgs L, SolveArgs A, 
     }
     // ---- bulk CTA: work items (step t, chunk q) over its share of the chunks; tiles by tensor-map
     // copies into two stage buffers, as in the forward kernel
-    const BulkRange R = bulk_range(L);
-    if (R.begin >= R.end || R.step <= 0) return;
+    const BulkRange Rg = bulk_range(L);
+    if (Rg.begin >= Rg.end || Rg.step <= 0) return;
     auto stage = [&](int k) { return k ? reinterpret_cast<T*>(Li) : Tl; };
     if (tid == 0) {
         bar_init(&sbar[0]);
@@ -693,8 +854,8 @@ __global__ void __launch_bounds__(256, 1) k_bwd_level(LevelArgs L, SolveArgs A, 
     unsigned phbits = 0;   // expected parity of each stage barrier
     auto next_item = [&](int& t, int& q) {
         for (;;) {
-            q = q < 0 ? R.begin : q + R.step;
-            if (q >= R.end) {
+            q = q < 0 ? Rg.begin : q + Rg.step;
+            if (q >= Rg.end) {
                 q = -1;
                 if (++t >= L.steps) return false;
                 continue;
@@ -708,7 +869,9 @@ __global__ void __launch_bounds__(256, 1) k_bwd_level(LevelArgs L, SolveArgs A, 
             start_bulk_tile<T, SB>(stage(st_), L.maps + L.bulk[q].s, (L.bulk[q].k0 - t) * SB, L.bulk[q].r0, &sbar[st_]);
     };
     int seen_blk = -1, seen_b = -1, prev_q = -1;
-    Cv gcur = Cv(0);   // g of this thread's column after the previous item (single right-hand side)
+    Cv gcur[FG];   // g of this thread's column after the previous item (all right-hand sides in one group)
+#pragma unroll
+    for (int j = 0; j < FG; ++j) gcur[j] = Cv(0);
     int t0 = 0, q0 = -1;
     if (!next_item(t0, q0)) return;
     int t1 = t0, q1 = q0;
@@ -722,39 +885,46 @@ __global__ void __launch_bounds__(256, 1) k_bwd_level(LevelArgs L, SolveArgs A, 
         const int b = c.k0 - t0, kb = min(SB, d.w - b * SB);
         const bool same = c.blk == seen_blk && b == seen_b;
         const int col = c.r0 + ccol;
+        const long long fo = A.fvec_off[c.s];
         // g of this thread's column, issued before the waits (this thread wrote it last, if anyone did)
-        Cv gold = Cv(0);
-        if (A.nrhs == 1 && cpart == 0 && col < c.r1) gold = q0 == prev_q ? gcur : fv[A.fvec_off[c.s] + col];
+        Cv gold[FG];
+#pragma unroll
+        for (int j = 0; j < FG; ++j) {
+            const int g = g0 + j;
+            gold[j] = (one_group && fin && col < c.r1 && g < nr)
+                          ? (q0 == prev_q ? gcur[j] : fv[fo + (long long)g * A.fv_stride + col])
+                          : Cv(0);
+        }
         if (!same && !wait_at_least(L.flags + c.blk + b, 1, L.status, &ok)) return;
-        for (int r = 0; r < A.nrhs; ++r) {
-            const long long base = A.fvec_off[c.s] + r * A.fv_stride;
-            Cv* g = fv + base;
-            if (!(same && A.nrhs == 1)) {
+        for (int rg = 0; rg < nr; rg += RG) {
+            const int ng = min(RG, nr - rg);
+            if (!(same && one_group)) {
                 __syncthreads();
-                for (int i = tid; i < SB; i += blockDim.x) xb[i] = i < kb ? __ldcg(xv + base + b * SB + i) : Cv(0);
+                load_x(fo, rg, ng, b, kb);
             }
-            if (r == 0) {
+            if (rg == 0) {
                 if (!__syncthreads_and(bar_wait(&sbar[cur], (phbits >> cur) & 1u, L.status))) return;
                 phbits ^= 1u << cur;
             }
             __syncthreads();
-            const T* tile = stage(cur);
-            // thread (column, part): its part of the rows in skewed order (bank-conflict free)
-            Cv acc = Cv(0);
-#pragma unroll 8
-            for (int u = 0; u < RPT; ++u) {
-                const int i = cpart * RPT + ((u + ccol) & (RPT - 1));
-                acc += (Cv)tile[i + ccol * SB] * xb[i];
-            }
-            part[tid] = acc;
+            RhsAcc<Cv, RG> acc;
+            acc.zero();
+            tile_t_x(acc, stage(cur));
+            acc.store(part + (cpart * SB + ccol) * RG);
             __syncthreads();
-            if (cpart == 0 && col < c.r1) {
-                Cv sum = part[ccol];
+            if (fin && col < c.r1) {
 #pragma unroll
-                for (int p = 1; p < TPC; ++p) sum += part[ccol + p * SB];
-                const Cv gv = (A.nrhs == 1 ? gold : g[col]) - sum;
-                g[col] = gv;
-                gcur = gv;
+                for (int j = 0; j < FG; ++j) {
+                    const int g = g0 + j;
+                    if (g >= ng) break;
+                    Cv sum = part[ccol * RG + g];
+#pragma unroll
+                    for (int p = 1; p < TPC; ++p) sum += part[(p * SB + ccol) * RG + g];
+                    Cv* gp = fv + fo + (long long)(rg + g) * A.fv_stride + col;
+                    const Cv gv = (one_group ? gold[j] : *gp) - sum;
+                    *gp = gv;
+                    gcur[j] = gv;
+                }
             }
         }
         seen_blk = c.blk;
@@ -930,18 +1100,19 @@ __global__ void k_bwd_gather(const SolveBlockTask* __restrict__ tasks, SolveArgs
     const int s = tk.s;
     const SnDev d = A.sn[s];
     const int* rows = A.rows + d.rows_off;
-    for (int r = 0; r < A.nrhs; ++r) {
+    for (int r = blockIdx.y; r < A.nrhs; r += gridDim.y) {
         Cv* g = fv + A.fvec_off[s] + r * A.fv_stride;
         for (int a = tk.r0 + threadIdx.x; a < tk.r1; a += blockDim.x) g[a] = work[rows[a] + (long long)r * A.ldw];
     }
 }
 
-// g[k] -= sum_{i in [r0, r1)} L[i,k] g[i] for columns k in [k0, k0+kn), one warp per column.
+// g[k] -= sum_{i in [r0, r1)} L[i,k] g[i] for columns k in [k0, k0+kn), one warp per column,
+// RG right-hand sides at a time (each column entry is loaded once per group).
 // Rows are read 16 bytes at a time between a scalar head and tail: a panel
 // column and the front vector start on 16-byte boundaries (panel offsets are
-// multiples of 64 elements, ldp and front-vector offsets of 8), so row i of
-// both is aligned exactly when i is a multiple of 16 / sizeof(element).
-template <class T, class Cv>
+// multiples of 64 elements, ldp, front-vector offsets and their stride of 8),
+// so row i of both is aligned exactly when i is a multiple of 16 / sizeof(element).
+template <class T, class Cv, int RG>
 __global__ void k_bwd_cols(const SolveBlockTask* __restrict__ tasks, SolveArgs A, const T* __restrict__ panel,
                            Cv* __restrict__ fv, Cv* __restrict__ partial) {
     static_assert(sizeof(T) == sizeof(Cv), "factor and vector elements of one size");
@@ -953,36 +1124,55 @@ __global__ void k_bwd_cols(const SolveBlockTask* __restrict__ tasks, SolveArgs A
     const SnDev d = A.sn[tk.s];
     const int k = tk.k0 + warp;
     const T* col = panel + d.panel_off + (long long)k * d.ldp;
+    const Vec* cv = reinterpret_cast<const Vec*>(col);
     const int head = min(tk.r1, (tk.r0 + V - 1) / V * V), body = max(head, tk.r1 / V * V);
-    for (int r = 0; r < A.nrhs; ++r) {
-        Cv* g = fv + A.fvec_off[tk.s] + r * A.fv_stride;
-        Cv acc = Cv(0);
-        for (int i = tk.r0 + lane; i < head; i += 32) acc += (Cv)col[i] * g[i];
-        const Vec* cv = reinterpret_cast<const Vec*>(col);
-        const Vec* gv = reinterpret_cast<const Vec*>(g);
+    auto dot = [](const Vec& a, const Vec& b) -> Cv {
+        if constexpr (V == 4) return (Cv)a.x * b.x + (Cv)a.y * b.y + (Cv)a.z * b.z + (Cv)a.w * b.w;
+        else return (Cv)a.x * b.x + (Cv)a.y * b.y;
+    };
+    for (int rg = 0; rg < A.nrhs; rg += RG) {
+        const int ng = min(RG, A.nrhs - rg);
+        Cv* g = fv + A.fvec_off[tk.s] + (long long)rg * A.fv_stride;
+        Cv acc[RG];
+#pragma unroll
+        for (int r = 0; r < RG; ++r) acc[r] = Cv(0);
+        for (int i = tk.r0 + lane; i < head; i += 32) {
+            const Cv a = (Cv)col[i];
+#pragma unroll
+            for (int r = 0; r < RG; ++r)
+                if (r < ng) acc[r] += a * g[r * A.fv_stride + i];
+        }
         int v = head / V + lane;
-        for (; v + 32 < body / V; v += 64) {   // two 16-byte loads of each in flight per lane
-            const Vec a0 = cv[v], a1 = cv[v + 32], b0 = gv[v], b1 = gv[v + 32];
-            if constexpr (V == 4) {
-                acc += (Cv)a0.x * b0.x + (Cv)a0.y * b0.y + (Cv)a0.z * b0.z + (Cv)a0.w * b0.w;
-                acc += (Cv)a1.x * b1.x + (Cv)a1.y * b1.y + (Cv)a1.z * b1.z + (Cv)a1.w * b1.w;
-            } else {
-                acc += (Cv)a0.x * b0.x + (Cv)a0.y * b0.y;
-                acc += (Cv)a1.x * b1.x + (Cv)a1.y * b1.y;
+        if constexpr (RG == 1) {
+            for (; v + 32 < body / V; v += 64) {   // two 16-byte loads of each in flight per lane
+                const Vec* gv = reinterpret_cast<const Vec*>(g);
+                const Vec a0 = cv[v], a1 = cv[v + 32], b0 = gv[v], b1 = gv[v + 32];
+                acc[0] += dot(a0, b0);
+                acc[0] += dot(a1, b1);
             }
         }
         for (; v < body / V; v += 32) {
-            const Vec a0 = cv[v], b0 = gv[v];
-            if constexpr (V == 4)
-                acc += (Cv)a0.x * b0.x + (Cv)a0.y * b0.y + (Cv)a0.z * b0.z + (Cv)a0.w * b0.w;
-            else
-                acc += (Cv)a0.x * b0.x + (Cv)a0.y * b0.y;
+            const Vec a = cv[v];
+#pragma unroll
+            for (int r = 0; r < RG; ++r)
+                if (r < ng) acc[r] += dot(a, reinterpret_cast<const Vec*>(g + r * A.fv_stride)[v]);
         }
-        for (int i = body + lane; i < tk.r1; i += 32) acc += (Cv)col[i] * g[i];
-        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        for (int i = body + lane; i < tk.r1; i += 32) {
+            const Cv a = (Cv)col[i];
+#pragma unroll
+            for (int r = 0; r < RG; ++r)
+                if (r < ng) acc[r] += a * g[r * A.fv_stride + i];
+        }
+#pragma unroll
+        for (int r = 0; r < RG; ++r)
+            for (int o = 16; o > 0; o >>= 1) acc[r] += __shfl_xor_sync(0xffffffffu, acc[r], o);
         if (lane == 0) {
-            if (tk.flags) partial[((long long)tk.blk * 8 + warp) * A.nrhs + r] = acc;   // one row chunk
-            else g[k] -= acc;
+#pragma unroll
+            for (int r = 0; r < RG; ++r) {
+                if (r >= ng) break;
+                if (tk.flags) partial[((long long)tk.blk * 8 + warp) * A.nrhs + rg + r] = acc[r];   // one row chunk
+                else g[r * A.fv_stride + k] -= acc[r];
+            }
         }
     }
 }

@@ -407,7 +407,9 @@ class UtduNumericFactorization:
         lib = _native.gpu()
         t = _native.PhaseTimes()
         raise_for_status(lib.uchol_factor_phase_times(self._h, C.byref(t)), lib.uchol_last_error())
-        return {name: getattr(t, name) for name, _ in _native.PhaseTimes._fields_}
+        out = {name: getattr(t, name) for name, _ in _native.PhaseTimes._fields_ if name != "solve_kind_ms"}
+        out["solve_ms"] = dict(zip(_native.SOLVE_KINDS, list(t.solve_kind_ms)))
+        return out
 
     def Refactorize(self, matrix: SymmetricCSRMatrix) -> None:
         """New values, same pattern, same device storage."""
@@ -513,6 +515,21 @@ class SymmetricUtduSolver(DirectLinearSolver):
         vals = np.ascontiguousarray(matrix.Values, np.float64)
         st = lib.uchol_factorize(h, matrix.Size, matrix.NonZeroCount, _native.ptr(vals, C.c_double), C.byref(opts),
                                  C.byref(out), C.byref(stats))
+        raise_for_status(st, lib.uchol_last_error())
+        return UtduNumericFactorization(symbolic, out, stats, self.Options, matrix)
+
+    def FactorizeDevice(self, matrix: SymmetricCSRMatrix, symbolic: UtduSymbolicFactorization, d_values: int):
+        """Factorize with the values already in device memory (pointer as an integer, the
+        matrix's value order); ``matrix`` supplies the pattern only."""
+        if matrix is None or symbolic is None:
+            raise ArgumentNullException("matrix" if matrix is None else "symbolic")
+        symbolic.EnsureCompatible(matrix)
+        lib = _native.gpu()
+        out = C.c_void_p()
+        stats = _native.FactorStats()
+        opts = self.Options._native_options()
+        st = lib.uchol_factorize_device(symbolic.device_handle(), matrix.Size, matrix.NonZeroCount,
+                                        C.c_void_p(d_values), C.byref(opts), C.byref(out), C.byref(stats))
         raise_for_status(st, lib.uchol_last_error())
         return UtduNumericFactorization(symbolic, out, stats, self.Options, matrix)
 
