@@ -98,6 +98,11 @@ typedef struct {
                                            when that adds at most 5% stored entries (exact zeros); the symbolic
                                            partition itself is unchanged.  0 = 1024, < 0 = one front per
                                            supernode. */
+    int inverse_block_width;            /* solves: fronts of more than one solve block (128 columns mixed, 64
+                                           FP64) and at most this many columns keep the inverse of their
+                                           diagonal block's unit-lower triangle (built after each
+                                           factorisation), so that their triangular solves are products
+                                           instead of a chain of block solves.  0 = 2048, < 0 = off. */
 } uchol_options;
 
 /* Pivot statistics (UtduNumericFactorization.cs:57-84) and timings. */
@@ -161,7 +166,7 @@ int uchol_solve_refined_device(uchol_factor f, int n, int nrhs, const double* d_
 int uchol_residual_norms(uchol_factor f, int n, int nrhs, const double* b, int ldb, const double* x, int ldx,
                          double* out_norms);
 
-#define UCHOL_SOLVE_KINDS 9
+#define UCHOL_SOLVE_KINDS 13
 
 /* Device-time of the last call on the handle's stream, per phase. */
 typedef struct {
@@ -174,7 +179,9 @@ typedef struct {
      * launches its kernels directly instead of replaying its graph).  Index: 0 forward
      * gather, 1 forward single-block fronts, 2 forward level kernels, 3 backward gather,
      * 4 backward column dots, 5 backward single-block fronts, 6 backward level kernels,
-     * 7 forward trailing rows of single-block fronts, 8 backward partial-sum reductions. */
+     * 7 forward trailing rows of single-block fronts, 8 backward partial-sum reductions,
+     * 9-12 inverse fronts: forward diagonal, forward trailing rows, backward partial sums,
+     * backward diagonal. */
     double solve_kind_ms[UCHOL_SOLVE_KINDS];
     double solve_total_ms;       /* sum over the solve's launches */
     int solve_launches;

@@ -25,6 +25,7 @@
 #include "plan.hpp"
 #include "solve_kernels.cuh"
 #include "tc_gemm.cuh"
+#include "inv_solve.cuh"
 
 using namespace uchol_dev;
 
@@ -115,7 +116,7 @@ struct DevPlan {
     Plan plan;
     DBuf sn, rel, asm_pos, ea_items, ea_entries, small, pivot_tasks, panel_tasks, simt_jobs, tc_jobs,
         stage;
-    DBuf fvec_off, solve_fronts, solve_tasks, inv_blocks;
+    DBuf fvec_off, solve_fronts, solve_tasks, inv_blocks, inv_tasks;
     DBuf rows, child_ptr, children;   // structure of the device fronts
 };
 
@@ -146,7 +147,7 @@ struct uchol_symbolic_s {
         std::string key = std::to_string(c.pivot_block) + "/" + std::to_string(c.outer_block) + "/" +
                           std::to_string(c.small_mask) + "/" + std::to_string(c.tensor_core) + "/" +
                           std::to_string(c.solve_block) + "/" + std::to_string(c.merge_cols) + "/" +
-                          std::to_string(c.merge_fill);
+                          std::to_string(c.merge_fill) + "/" + std::to_string(c.inv_cols);
         auto it = plans.find(key);
         if (it != plans.end()) return it->second.get();
         auto dp = std::make_unique<DevPlan>();
@@ -173,6 +174,7 @@ struct uchol_symbolic_s {
         dp->solve_fronts.upload(P.solve_fronts, stream, "plan");
         dp->solve_tasks.upload(P.solve_tasks, stream, "plan");
         dp->inv_blocks.upload(P.inv_blocks, stream, "plan");
+        dp->inv_tasks.upload(P.inv_tasks, stream, "plan");
         dp->rows.upload(P.front_rows, stream, "front rows");
         dp->child_ptr.upload(P.child_ptr, stream, "children");
         dp->children.upload(P.children, stream, "children");
@@ -193,6 +195,8 @@ struct uchol_factor_s {
     DBuf work, fv, fv2, vec[6], scal;   // solve workspace
     DBuf bwd_partial;                   // backward column dots split in row chunks: partial sums
     DBuf linv;                          // inverses of the diagonal blocks (solves)
+    DBuf linv_off;                      // inverse fronts: off-diagonal blocks of the diagonal block's inverse
+    DBuf inv_partial;                   // inverse fronts: backward partial sums (solve workspace)
     DBuf minv;                          // mixed path: per outer block X^T, D, D^{-1} of each diagonal block
     DBuf solve_flags;                   // per diagonal block: forward and backward "solution published" flags
     DBuf solve_maps;                    // per supernode: tensor map of the diagonal region of its panel
@@ -258,6 +262,7 @@ PlanConfig config_for(const uchol_options& o) {
     c.small_mask = o.small_front_buckets ? o.small_front_buckets : 0x7;
     c.pivot_block = std::min(kMaxPivotBlock, std::max(4, std::min(128, o.panel_width)));
     c.merge_cols = o.chain_merge_width == 0 ? kDefaultMergeCols : std::max(0, o.chain_merge_width);
+    c.inv_cols = o.inverse_block_width == 0 ? kDefaultInvCols : std::max(0, o.inverse_block_width);
     if (o.precision == UCHOL_PRECISION_FP64) {
         c.tensor_core = false;
         c.outer_block = c.pivot_block;
@@ -418,10 +423,14 @@ void prepare_factor_kernels(uchol_factor_s* F) {
         CK(cudaFuncSetAttribute(k_small_fronts<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, std::max(small, 1)));
         CK(cudaFuncSetAttribute(k_invert_blocks<double, double, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)(2 * 64 * 64 * sizeof(double))));
+        CK(cudaFuncSetAttribute(k_inv_offdiag<double, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)inv_offdiag_smem<double, 64>()));
     } else {
         CK(cudaFuncSetAttribute(k_small_fronts<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, std::max(small, 1)));
         CK(cudaFuncSetAttribute(k_invert_blocks<float, float, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)(2 * 128 * 128 * sizeof(float))));
+        CK(cudaFuncSetAttribute(k_inv_offdiag<float, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)inv_offdiag_smem<float, 128>()));
         CK(cudaFuncSetAttribute(k_diag_block, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDiagSmemBytes));
         CK(cudaFuncSetAttribute(k_panel_solve<__nv_bfloat16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)kPanelSmemBytes));
@@ -443,11 +452,24 @@ void invert_diagonal_blocks(uchol_factor_s* F, cudaStream_t st) {
         const size_t smem = 2 * SB * SB * sizeof(double);
         k_invert_blocks<double, double, SB><<<nb, SB, smem, st>>>(D.inv_blocks.as<SolveBlockTask>(), D.sn.as<SnDev>(),
                                                                   F->panel.as<double>(), F->linv.as<double>());
+        // inverse fronts: off-diagonal blocks of the inverse, one launch per block diagonal
+        for (const InvLaunch& L : P.inv_launches) {
+            k_inv_offdiag<double, SB><<<L.count, 256, inv_offdiag_smem<double, SB>(), st>>>(
+                D.inv_tasks.as<SolveBlockTask>() + L.begin, D.sn.as<SnDev>(), F->panel.as<double>(),
+                F->linv.as<double>(), F->linv_off.as<double>());
+            counted();
+        }
     } else {
         constexpr int SB = 128;
         const size_t smem = 2 * SB * SB * sizeof(float);
         k_invert_blocks<float, float, SB><<<nb, SB, smem, st>>>(D.inv_blocks.as<SolveBlockTask>(), D.sn.as<SnDev>(),
                                                                 F->panel.as<float>(), F->linv.as<float>());
+        for (const InvLaunch& L : P.inv_launches) {
+            k_inv_offdiag<float, SB><<<L.count, 256, inv_offdiag_smem<float, SB>(), st>>>(
+                D.inv_tasks.as<SolveBlockTask>() + L.begin, D.sn.as<SnDev>(), F->panel.as<float>(),
+                F->linv.as<float>(), F->linv_off.as<float>());
+            counted();
+        }
     }
     counted();
     CK(cudaGetLastError());
@@ -646,6 +668,8 @@ uchol_factor_s* create_factor(uchol_symbolic_s* S, int n, int nnz, const uchol_o
     F->diag.alloc((size_t)std::max(1, S->n) * sizeof(double), "pivots");
     F->linv.alloc((size_t)std::max<size_t>(1, P.inv_blocks.size()) * cfg.solve_block * cfg.solve_block * F->elem,
                   "inverse diagonal blocks");
+    F->linv_off.alloc((size_t)std::max<long long>(1, P.inv_off_blocks) * cfg.solve_block * cfg.solve_block * F->elem,
+                      "inverse blocks of the inverse fronts");
     F->values.alloc((size_t)std::max(1, S->nnz) * sizeof(double), "matrix values");
     F->full_val.alloc((size_t)std::max<long long>(1, S->full_nnz) * sizeof(double), "matrix values");
     F->stats.alloc(sizeof(PivotStats), "statistics");
@@ -746,6 +770,7 @@ void run_solve(uchol_factor_s* F, int nrhs, Cv* work, Cv* fv, Cv* fv2, cudaStrea
     int* status = F->solve_status.as<int>();
     CK(cudaMemsetAsync(fwd_flags, 0, sizeof(int) * ((size_t)2 * nblocks + P.progress_count), st));
     const size_t smem = level_smem_bytes<T, Cv, SB, RG>();
+    constexpr int RGD = RG == 1 ? 1 : 4;   // right-hand sides per CTA of the inverse-front diagonal kernels
     auto level_args = [&](const SolveLaunch& L, int* flags, int grid) {
         LevelArgs la;
         la.chains = tasks + L.begin;
@@ -784,6 +809,12 @@ void run_solve(uchol_factor_s* F, int nrhs, Cv* work, Cv* fv, Cv* fv2, cudaStrea
             k_fwd_gather<Cv><<<dim3(L.count, std::min(nrhs, 65535)), 256, 0, st>>>(tasks + L.begin, A, work, fv);
         } else if (L.kind == SolveLaunch::FwdSolo) {
             k_fwd_solo<T, Cv, SB><<<L.count, 256, 0, st>>>(tasks + L.begin, A, panel, linv, fv, fv2, diag, work);
+        } else if (L.kind == SolveLaunch::FwdInvDiag) {
+            k_fwd_inv_diag<T, Cv, SB, RGD><<<dim3(L.count, (nrhs + RGD - 1) / RGD), 256, inv_solve_smem<T, Cv, SB, RGD>(), st>>>(
+                tasks + L.begin, A, linv, F->linv_off.as<Cv>(), fv, fv2, diag, work, status);
+        } else if (L.kind == SolveLaunch::FwdInvTail) {
+            k_fwd_inv_tail<T, Cv, SB, RG><<<L.count, 256, inv_solve_smem<T, Cv, SB, RG>(), st>>>(
+                tasks + L.begin, A, F->solve_maps.as<CUtensorMap>(), fv2, fv, status);
         } else if (L.kind == SolveLaunch::FwdTail) {
             if (nrhs == 1)
                 k_fwd_tail<T, Cv, SB, 1><<<L.count, kTailRows / 4, 0, st>>>(tasks + L.begin, A, panel, fv2, fv);
@@ -805,6 +836,12 @@ void run_solve(uchol_factor_s* F, int nrhs, Cv* work, Cv* fv, Cv* fv2, cudaStrea
             k_bwd_cols<T, Cv, RG><<<L.count, 256, 0, st>>>(tasks + L.begin, A, panel, fv, F->bwd_partial.as<Cv>());
         } else if (L.kind == SolveLaunch::BwdTailReduce) {
             k_bwd_cols_reduce<Cv><<<L.count, 128, 0, st>>>(tasks + L.begin, A, F->bwd_partial.as<Cv>(), fv);
+        } else if (L.kind == SolveLaunch::BwdInvCols) {
+            k_bwd_inv_cols<T, Cv, SB, RG><<<L.count, 256, inv_solve_smem<T, Cv, SB, RG>(), st>>>(
+                tasks + L.begin, A, F->solve_maps.as<CUtensorMap>(), fv, F->inv_partial.as<Cv>(), status);
+        } else if (L.kind == SolveLaunch::BwdInvDiag) {
+            k_bwd_inv_diag<T, Cv, SB, RGD><<<dim3(L.count, (nrhs + RGD - 1) / RGD), 256, inv_solve_smem<T, Cv, SB, RGD>(), st>>>(
+                tasks + L.begin, A, linv, F->linv_off.as<Cv>(), fv, F->inv_partial.as<Cv>(), work, status);
         } else if (L.kind == SolveLaunch::BwdSolo) {
             k_bwd_solo<Cv, SB><<<L.count, 256, 0, st>>>(tasks + L.begin, A, linv, fv, fv2, work);
         } else {
@@ -851,6 +888,23 @@ void launch_solve_graph(uchol_factor_s* F, int nrhs, Cv* work, cudaStream_t st) 
         else
             level_kernels(k_fwd_level<T, Cv, SB, kSolveRhsGroup>, k_bwd_level<T, Cv, SB, kSolveRhsGroup>,
                           (int)level_smem_bytes<T, Cv, SB, kSolveRhsGroup>());
+        // inverse-front kernels of both groupings
+        CK(cudaFuncSetAttribute(k_fwd_inv_diag<T, Cv, SB, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)inv_solve_smem<T, Cv, SB, 1>()));
+        CK(cudaFuncSetAttribute(k_fwd_inv_diag<T, Cv, SB, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)inv_solve_smem<T, Cv, SB, 4>()));
+        CK(cudaFuncSetAttribute(k_bwd_inv_diag<T, Cv, SB, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)inv_solve_smem<T, Cv, SB, 1>()));
+        CK(cudaFuncSetAttribute(k_bwd_inv_diag<T, Cv, SB, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)inv_solve_smem<T, Cv, SB, 4>()));
+        CK(cudaFuncSetAttribute(k_fwd_inv_tail<T, Cv, SB, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)inv_solve_smem<T, Cv, SB, 1>()));
+        CK(cudaFuncSetAttribute(k_fwd_inv_tail<T, Cv, SB, kSolveRhsGroup>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)inv_solve_smem<T, Cv, SB, kSolveRhsGroup>()));
+        CK(cudaFuncSetAttribute(k_bwd_inv_cols<T, Cv, SB, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)inv_solve_smem<T, Cv, SB, 1>()));
+        CK(cudaFuncSetAttribute(k_bwd_inv_cols<T, Cv, SB, kSolveRhsGroup>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)inv_solve_smem<T, Cv, SB, kSolveRhsGroup>()));
         if (F->coop_fwd < 2 || F->coop_bwd < 2) throw Error(UCHOL_CUDA_ERROR, "the level solve kernels do not fit");
         if (!F->solve_maps.p) {
             // tile copies of the level solves: each front's panel (m x w)
@@ -925,6 +979,7 @@ void ensure_workspace(uchol_factor_s* F, int nrhs) {
     F->fv.alloc((size_t)P.fvec_elems * nrhs * cv, "solve workspace");
     F->fv2.alloc((size_t)P.fvec_elems * nrhs * cv, "solve workspace");
     F->bwd_partial.alloc((size_t)std::max(1, P.bwd_partial_slots) * 8 * nrhs * cv, "solve workspace");
+    F->inv_partial.alloc((size_t)std::max(1, P.inv_partial_slots) * P.cfg.solve_block * nrhs * cv, "solve workspace");
     if (F->solve_graph) {
         CK(cudaGraphExecDestroy(F->solve_graph));
         F->solve_graph = nullptr;
@@ -1101,6 +1156,7 @@ void uchol_default_options(uchol_options* o) {
     o->block_width = 0;
     o->small_front_buckets = 0;
     o->chain_merge_width = 0;
+    o->inverse_block_width = 0;
 }
 
 int uchol_symbolic_create(const uchol_symbolic_desc* d, uchol_symbolic* out) {

@@ -1,0 +1,430 @@
+// Solves of inverse fronts: fronts of solve_block < w <= inv_cols columns keep
+// the whole inverse of the unit-lower triangle of their diagonal block, so that
+// a level's solve needs no chain of block solves.  Forward, per front:
+//   y_1 = Linv_11 f_1                  (k_fwd_inv_diag: one CTA per block row),
+//   f_2 -= L_21 y_1                    (k_fwd_inv_tail: one CTA per chunk of trailing rows);
+// backward:
+//   g_1 -= L_21^T g_2                  (k_bwd_inv_cols: partial sums per chunk of rows),
+//   x_1 = Linv_11^T g_1                (k_bwd_inv_diag: adds the partial sums in order).
+// The algebra is the reference's supernodal substitution
+// (CAESolvers/UCHOL/UtduNumericFactorization.cs:139-207) with the triangular solve of
+// the diagonal block written as a product with its inverse; the result differs only
+// in rounding.  The inverse is built once per factorisation from the inverses of the
+// SB x SB diagonal blocks (k_invert_blocks): block (i, j), i > j, is
+// -Linv(i, i) sum_{j <= k < i} L(i, k) Linv(k, j), by increasing i - j (k_inv_offdiag).
+#pragma once
+
+#include "solve_kernels.cuh"
+
+namespace uchol_dev {
+
+// SB x SB block of the inverse, column-major: (i, i) in the diagonal-block arena, (i, j), i > j,
+// in the off-diagonal arena.
+template <class Cv, int SB>
+__device__ __forceinline__ const Cv* inv_block(const Cv* linv, const Cv* linv_off, int blk, int ob, int i, int j) {
+    return i == j ? linv + (long long)(blk + i) * SB * SB
+                  : linv_off + ((long long)ob + (long long)i * (i - 1) / 2 + j) * SB * SB;
+}
+
+// C (SB x SB, in registers: thread (tx, ty) holds rows tx TM .. +TM, columns ty TN .. +TN)
+// += A B for column-major SB x SB A and B in shared memory.
+template <class T, int SB>
+struct BlockGemm {
+    static constexpr int TM = SB / 16, TN = SB / 16;
+    T c[TM][TN];
+    __device__ __forceinline__ void zero() {
+#pragma unroll
+        for (int a = 0; a < TM; ++a)
+#pragma unroll
+            for (int b = 0; b < TN; ++b) c[a][b] = T(0);
+    }
+    __device__ __forceinline__ void mma(const T* A, const T* B, int tx, int ty) {
+#pragma unroll 4
+        for (int kk = 0; kk < SB; ++kk) {
+            T a[TM], b[TN];
+#pragma unroll
+            for (int u = 0; u < TM; ++u) a[u] = A[tx * TM + u + kk * SB];
+#pragma unroll
+            for (int v = 0; v < TN; ++v) b[v] = B[kk + (ty * TN + v) * SB];
+#pragma unroll
+            for (int u = 0; u < TM; ++u)
+#pragma unroll
+                for (int v = 0; v < TN; ++v) c[u][v] += a[u] * b[v];
+        }
+    }
+};
+
+// Off-diagonal inverse block (i, j) of an inverse front (task {s, i, j, ob, -, -, blk}).
+template <class T, int SB>
+__global__ void __launch_bounds__(256) k_inv_offdiag(const SolveBlockTask* __restrict__ tasks, const SnDev* __restrict__ sn,
+                                                     const T* __restrict__ panel, const T* __restrict__ linv,
+                                                     T* __restrict__ linv_off) {
+    extern __shared__ __align__(16) unsigned char inv_smem[];
+    T* A = reinterpret_cast<T*>(inv_smem);
+    T* B = A + SB * SB;
+    const SolveBlockTask tk = tasks[blockIdx.x];
+    const SnDev d = sn[tk.s];
+    const int i = tk.k0, j = tk.kn, ob = tk.r0, blk = tk.blk;
+    const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
+    const T* P = panel + d.panel_off;
+    BlockGemm<T, SB> g;
+    g.zero();
+    for (int k = j; k < i; ++k) {
+        __syncthreads();
+        // A = L(i, k), rows past the front's columns (its trailing rows) read as zero
+        for (int e = tid; e < SB * SB; e += blockDim.x) {
+            const int r = e % SB, c = e / SB, gr = i * SB + r;
+            A[e] = gr < d.w ? P[gr + (long long)(k * SB + c) * d.ldp] : T(0);
+        }
+        const T* Bk = inv_block<T, SB>(linv, linv_off, blk, ob, k, j);
+        for (int e = tid; e < SB * SB; e += blockDim.x) B[e] = Bk[e];
+        __syncthreads();
+        g.mma(A, B, tx, ty);
+    }
+    // X = the sum, into B; then -Linv(i, i) X
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < BlockGemm<T, SB>::TM; ++u)
+#pragma unroll
+        for (int v = 0; v < BlockGemm<T, SB>::TN; ++v)
+            B[tx * BlockGemm<T, SB>::TM + u + (ty * BlockGemm<T, SB>::TN + v) * SB] = g.c[u][v];
+    const T* Di = linv + (long long)(blk + i) * SB * SB;
+    for (int e = tid; e < SB * SB; e += blockDim.x) A[e] = Di[e];
+    __syncthreads();
+    g.zero();
+    g.mma(A, B, tx, ty);
+    T* out = linv_off + ((long long)ob + (long long)i * (i - 1) / 2 + j) * SB * SB;
+#pragma unroll
+    for (int u = 0; u < BlockGemm<T, SB>::TM; ++u)
+#pragma unroll
+        for (int v = 0; v < BlockGemm<T, SB>::TN; ++v)
+            out[tx * BlockGemm<T, SB>::TM + u + (ty * BlockGemm<T, SB>::TN + v) * SB] = -g.c[u][v];
+}
+
+template <class T, int SB>
+constexpr size_t inv_offdiag_smem() { return (size_t)2 * SB * SB * sizeof(T); }
+
+// Shared memory of the inverse-front solve kernels: two SB x SB tile stages, a
+// right-hand block (SB rows x RG, stride RS) and the partial sums.
+template <class T, class Cv, int SB, int RG>
+constexpr size_t inv_solve_smem() {
+    return (size_t)2 * SB * SB * sizeof(T) + LevelRhs<Cv, SB, RG>::bytes + kLevelSmemSlack;
+}
+
+// Forward y_i = sum_{j <= i} Linv(i, j) f_j for right-hand sides [RG blockIdx.y, +RG);
+// writes y_i (front vector yv) and y_i / D (work).  Thread (row, pid) sums columns
+// [pid CPT, pid CPT + CPT) of each block.
+template <class T, class Cv, int SB, int RG>
+__global__ void __launch_bounds__(256, 1) k_fwd_inv_diag(const SolveBlockTask* __restrict__ tasks, SolveArgs A,
+                                                         const Cv* __restrict__ linv, const Cv* __restrict__ linv_off,
+                                                         const Cv* __restrict__ fv, Cv* __restrict__ yv,
+                                                         const double* __restrict__ diag, Cv* __restrict__ work,
+                                                         int* status) {
+    using R = LevelRhs<Cv, SB, RG>;
+    constexpr int TPR = R::TP, CPT = SB / TPR, RS = R::RS, FG = R::FG;
+    extern __shared__ __align__(128) unsigned char blk_smem[];
+    unsigned char* sm = blk_smem + ((1024u - (smem_addr(blk_smem) & 1023u)) & 1023u);
+    Cv* const stage0 = reinterpret_cast<Cv*>(sm);        // two Linv tile stages
+    auto stage = [&](int k) { return stage0 + k * SB * SB; };
+    Cv* fb = stage0 + 2 * SB * SB;                       // f_j: SB rows x RG
+    Cv* part = fb + 2 * SB * RS;
+    __shared__ unsigned long long bar[2];
+    const SolveBlockTask tk = tasks[blockIdx.x];
+    const SnDev d = A.sn[tk.s];
+    const int i = tk.k0, ob = tk.r0, blk = tk.blk;
+    const int rg = blockIdx.y * RG, ng = min(RG, A.nrhs - rg);
+    const int tid = threadIdx.x, row = tid % SB, pid = tid / SB;
+    const bool fin = RG >= TPR || pid == 0;
+    const int g0 = RG >= TPR ? pid * FG : 0;
+    const long long fo = A.fvec_off[tk.s];
+    if (tid == 0) {
+        bar_init(&bar[0]);
+        bar_init(&bar[1]);
+    }
+    __syncthreads();
+    constexpr unsigned kTileBytes = SB * SB * sizeof(Cv);
+    auto issue = [&](int jj) {
+        if (tid == 0) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            bar_expect(&bar[jj & 1], kTileBytes);
+            bulk_g2s(stage(jj & 1), inv_block<Cv, SB>(linv, linv_off, blk, ob, i, jj), kTileBytes, &bar[jj & 1]);
+        }
+    };
+    issue(0);
+    if (i >= 1) issue(1);
+    RhsAcc<Cv, RG> acc;
+    acc.zero();
+    unsigned phase = 0;
+    for (int j = 0; j <= i; ++j) {
+        // f_j, zero past the front's columns and the group's right-hand sides
+        for (int e = tid; e < SB * RG; e += blockDim.x) {
+            const int g = e / SB, c = e - g * SB, col = j * SB + c;
+            fb[c * RS + g] = (g < ng && col < d.w) ? fv[fo + (long long)(rg + g) * A.fv_stride + col] : Cv(0);
+        }
+        if (!__syncthreads_and(bar_wait(&bar[j & 1], (phase >> (j & 1)) & 1u, status))) return;
+        phase ^= 1u << (j & 1);
+        const Cv* tile = stage(j & 1);
+#pragma unroll 2
+        for (int u0 = 0; u0 < CPT; u0 += 4)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int c = pid * CPT + u0 + q;
+                acc.add(q, tile[row + c * SB], fb + c * RS);
+            }
+        __syncthreads();   // the stage and fb are free again
+        if (j + 2 <= i) issue(j + 2);
+    }
+    acc.store(part + (pid * SB + row) * RG);
+    __syncthreads();
+    if (fin) {
+        const int kn = min(SB, d.w - i * SB);
+#pragma unroll
+        for (int q = 0; q < FG; ++q) {
+            const int g = g0 + q;
+            if (g >= ng || row >= kn) break;
+            Cv y = part[row * RG + g];
+#pragma unroll
+            for (int p = 1; p < TPR; ++p) y += part[(p * SB + row) * RG + g];
+            const int col = i * SB + row;
+            yv[fo + (long long)(rg + g) * A.fv_stride + col] = y;
+            work[d.first_col + col + (long long)(rg + g) * A.ldw] = (Cv)((double)y / diag[d.first_col + col]);
+        }
+    }
+}
+
+// Forward trailing rows [r0, r1) of an inverse front: f -= L[r0:r1, 0:w] y, tile by
+// tile (tensor-map copies, two stages); the tiles start at r0 rounded down to 16 bytes.
+template <class T, class Cv, int SB, int RG>
+__global__ void __launch_bounds__(256, 1) k_fwd_inv_tail(const SolveBlockTask* __restrict__ tasks, SolveArgs A,
+                                                         const CUtensorMap* __restrict__ maps,
+                                                         const Cv* __restrict__ yv, Cv* __restrict__ fv, int* status) {
+    using R = LevelRhs<Cv, SB, RG>;
+    constexpr int TPR = R::TP, CPT = SB / TPR, RS = R::RS, FG = R::FG;
+    constexpr int kAlign = 16 / (int)sizeof(T);
+    extern __shared__ __align__(128) unsigned char blk_smem[];
+    unsigned char* sm = blk_smem + ((1024u - (smem_addr(blk_smem) & 1023u)) & 1023u);
+    T* const stage0 = reinterpret_cast<T*>(sm);          // two tile stages
+    auto stage = [&](int k) { return stage0 + k * SB * SB; };
+    Cv* yb = reinterpret_cast<Cv*>(stage0 + 2 * SB * SB);
+    Cv* part = yb + 2 * SB * RS;
+    __shared__ unsigned long long bar[2];
+    const SolveBlockTask tk = tasks[blockIdx.x];
+    const SnDev d = A.sn[tk.s];
+    const int nb = tk.kn, r0 = tk.r0, r1 = tk.r1, ra = r0 & ~(kAlign - 1);
+    const int tid = threadIdx.x, row = tid % SB, pid = tid / SB;
+    const bool fin = RG >= TPR || pid == 0;
+    const int g0 = RG >= TPR ? pid * FG : 0;
+    const int i = r0 + row, trow = min(row + (r0 - ra), SB - 1);
+    const long long fo = A.fvec_off[tk.s];
+    if (tid == 0) {
+        bar_init(&bar[0]);
+        bar_init(&bar[1]);
+    }
+    __syncthreads();
+    unsigned phase = 0;
+    for (int rg = 0; rg < A.nrhs; rg += RG) {
+        const int ng = min(RG, A.nrhs - rg);
+        if (tid == 0) {
+            start_bulk_tile<T, SB>(stage(0), maps + tk.s, ra, 0, &bar[0]);
+            if (nb > 1) start_bulk_tile<T, SB>(stage(1), maps + tk.s, ra, SB, &bar[1]);
+        }
+        RhsAcc<Cv, RG> acc;
+        acc.zero();
+        for (int kb = 0; kb < nb; ++kb) {
+            const int kn = min(SB, d.w - kb * SB);
+            for (int e = tid; e < SB * RG; e += blockDim.x) {
+                const int g = e / SB, c = e - g * SB;
+                yb[c * RS + g] = (g < ng && c < kn) ? yv[fo + (long long)(rg + g) * A.fv_stride + kb * SB + c] : Cv(0);
+            }
+            if (!__syncthreads_and(bar_wait(&bar[kb & 1], (phase >> (kb & 1)) & 1u, status))) return;
+            phase ^= 1u << (kb & 1);
+            const T* tile = stage(kb & 1);
+#pragma unroll 2
+            for (int u0 = 0; u0 < CPT; u0 += 4)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int c = pid * CPT + u0 + q;
+                    acc.add(q, (Cv)tile[trow + c * SB], yb + c * RS);
+                }
+            __syncthreads();   // the stage and yb are free again
+            if (tid == 0 && kb + 2 < nb) start_bulk_tile<T, SB>(stage(kb & 1), maps + tk.s, ra, (kb + 2) * SB, &bar[kb & 1]);
+        }
+        acc.store(part + (pid * SB + row) * RG);
+        __syncthreads();
+        if (fin && i < r1) {
+#pragma unroll
+            for (int q = 0; q < FG; ++q) {
+                const int g = g0 + q;
+                if (g >= ng) break;
+                Cv sum = part[row * RG + g];
+#pragma unroll
+                for (int p = 1; p < TPR; ++p) sum += part[(p * SB + row) * RG + g];
+                fv[fo + (long long)(rg + g) * A.fv_stride + i] -= sum;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// Backward partial sums of column block kb of an inverse front against its trailing rows
+// [r0, r1): partial[(slot nrhs + r) SB + c] = sum_rows L[row, kb SB + c] g[row] (right-hand
+// side r).  Thread (column, part) sums its part of each tile's rows in skewed order.
+template <class T, class Cv, int SB, int RG>
+__global__ void __launch_bounds__(256, 1) k_bwd_inv_cols(const SolveBlockTask* __restrict__ tasks, SolveArgs A,
+                                                         const CUtensorMap* __restrict__ maps,
+                                                         const Cv* __restrict__ fv, Cv* __restrict__ partial,
+                                                         int* status) {
+    using R = LevelRhs<Cv, SB, RG>;
+    constexpr int TPC = R::TP, RPT = SB / TPC, RS = R::RS, FG = R::FG;
+    constexpr int kAlign = 16 / (int)sizeof(T);
+    extern __shared__ __align__(128) unsigned char blk_smem[];
+    unsigned char* sm = blk_smem + ((1024u - (smem_addr(blk_smem) & 1023u)) & 1023u);
+    T* const stage0 = reinterpret_cast<T*>(sm);          // two tile stages
+    auto stage = [&](int k) { return stage0 + k * SB * SB; };
+    Cv* xb = reinterpret_cast<Cv*>(stage0 + 2 * SB * SB);
+    Cv* part = xb + 2 * SB * RS;
+    __shared__ unsigned long long bar[2];
+    const SolveBlockTask tk = tasks[blockIdx.x];
+    const int kb = tk.k0, r0 = tk.r0, r1 = tk.r1, ra = r0 & ~(kAlign - 1);
+    const int ntile = (r1 - ra + SB - 1) / SB;
+    const int tid = threadIdx.x, ccol = tid % SB, cpart = tid / SB;
+    const bool fin = RG >= TPC || cpart == 0;
+    const int g0 = RG >= TPC ? cpart * FG : 0;
+    const long long fo = A.fvec_off[tk.s];
+    if (tid == 0) {
+        bar_init(&bar[0]);
+        bar_init(&bar[1]);
+    }
+    __syncthreads();
+    unsigned phase = 0;
+    for (int rg = 0; rg < A.nrhs; rg += RG) {
+        const int ng = min(RG, A.nrhs - rg);
+        if (tid == 0) {
+            start_bulk_tile<T, SB>(stage(0), maps + tk.s, ra, kb * SB, &bar[0]);
+            if (ntile > 1) start_bulk_tile<T, SB>(stage(1), maps + tk.s, ra + SB, kb * SB, &bar[1]);
+        }
+        RhsAcc<Cv, RG> acc;
+        acc.zero();
+        for (int t = 0; t < ntile; ++t) {
+            const int tr = ra + t * SB;
+            for (int e = tid; e < SB * RG; e += blockDim.x) {
+                const int g = e / SB, r = e - g * SB, gr = tr + r;
+                xb[r * RS + g] =
+                    (g < ng && gr >= r0 && gr < r1) ? fv[fo + (long long)(rg + g) * A.fv_stride + gr] : Cv(0);
+            }
+            if (!__syncthreads_and(bar_wait(&bar[t & 1], (phase >> (t & 1)) & 1u, status))) return;
+            phase ^= 1u << (t & 1);
+            const T* tile = stage(t & 1);
+#pragma unroll 2
+            for (int u0 = 0; u0 < RPT; u0 += 4)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int r = cpart * RPT + ((u0 + q + ccol) & (RPT - 1));
+                    acc.add(q, (Cv)tile[r + ccol * SB], xb + r * RS);
+                }
+            __syncthreads();
+            if (tid == 0 && t + 2 < ntile) start_bulk_tile<T, SB>(stage(t & 1), maps + tk.s, ra + (t + 2) * SB, kb * SB, &bar[t & 1]);
+        }
+        acc.store(part + (cpart * SB + ccol) * RG);
+        __syncthreads();
+        if (fin) {
+#pragma unroll
+            for (int q = 0; q < FG; ++q) {
+                const int g = g0 + q;
+                if (g >= ng) break;
+                Cv sum = part[ccol * RG + g];
+#pragma unroll
+                for (int p = 1; p < TPC; ++p) sum += part[(p * SB + ccol) * RG + g];
+                partial[((long long)tk.blk * A.nrhs + rg + g) * SB + ccol] = sum;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// Backward x_j = sum_{i >= j} Linv(i, j)^T g_i, g_i = the gathered block minus its nq partial
+// sums (slots slot0 + i nq + q, added in order), right-hand sides [RG blockIdx.y, +RG);
+// writes x_j to the work vector.
+template <class T, class Cv, int SB, int RG>
+__global__ void __launch_bounds__(256, 1) k_bwd_inv_diag(const SolveBlockTask* __restrict__ tasks, SolveArgs A,
+                                                         const Cv* __restrict__ linv, const Cv* __restrict__ linv_off,
+                                                         const Cv* __restrict__ fv, const Cv* __restrict__ partial,
+                                                         Cv* __restrict__ work, int* status) {
+    using R = LevelRhs<Cv, SB, RG>;
+    constexpr int TPC = R::TP, RPT = SB / TPC, RS = R::RS, FG = R::FG;
+    extern __shared__ __align__(128) unsigned char blk_smem[];
+    unsigned char* sm = blk_smem + ((1024u - (smem_addr(blk_smem) & 1023u)) & 1023u);
+    Cv* const stage0 = reinterpret_cast<Cv*>(sm);        // two Linv tile stages
+    auto stage = [&](int k) { return stage0 + k * SB * SB; };
+    Cv* gb = stage0 + 2 * SB * SB;
+    Cv* part = gb + 2 * SB * RS;
+    __shared__ unsigned long long bar[2];
+    const SolveBlockTask tk = tasks[blockIdx.x];
+    const SnDev d = A.sn[tk.s];
+    const int j = tk.k0, nb = tk.kn, ob = tk.r0, slot0 = tk.r1, nq = tk.flags, blk = tk.blk;
+    const int rg = blockIdx.y * RG, ng = min(RG, A.nrhs - rg);
+    const int tid = threadIdx.x, ccol = tid % SB, cpart = tid / SB;
+    const bool fin = RG >= TPC || cpart == 0;
+    const int g0 = RG >= TPC ? cpart * FG : 0;
+    const long long fo = A.fvec_off[tk.s];
+    if (tid == 0) {
+        bar_init(&bar[0]);
+        bar_init(&bar[1]);
+    }
+    __syncthreads();
+    constexpr unsigned kTileBytes = SB * SB * sizeof(Cv);
+    auto issue = [&](int ii) {
+        if (tid == 0) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            const int st = (ii - j) & 1;
+            bar_expect(&bar[st], kTileBytes);
+            bulk_g2s(stage(st), inv_block<Cv, SB>(linv, linv_off, blk, ob, ii, j), kTileBytes, &bar[st]);
+        }
+    };
+    issue(j);
+    if (j + 1 < nb) issue(j + 1);
+    RhsAcc<Cv, RG> acc;
+    acc.zero();
+    unsigned phase = 0;
+    for (int i = j; i < nb; ++i) {
+        const int st = (i - j) & 1;
+        for (int e = tid; e < SB * RG; e += blockDim.x) {
+            const int g = e / SB, c = e - g * SB, col = i * SB + c;
+            Cv v = Cv(0);
+            if (g < ng && col < d.w) {
+                v = fv[fo + (long long)(rg + g) * A.fv_stride + col];
+                const Cv* pp = partial + ((long long)(slot0 + i * nq) * A.nrhs + rg + g) * SB + c;
+                for (int q = 0; q < nq; ++q) v -= pp[(long long)q * A.nrhs * SB];
+            }
+            gb[c * RS + g] = v;
+        }
+        if (!__syncthreads_and(bar_wait(&bar[st], (phase >> st) & 1u, status))) return;
+        phase ^= 1u << st;
+        const Cv* tile = stage(st);
+#pragma unroll 2
+        for (int u0 = 0; u0 < RPT; u0 += 4)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int c = cpart * RPT + ((u0 + q + ccol) & (RPT - 1));
+                acc.add(q, tile[c + ccol * SB], gb + c * RS);
+            }
+        __syncthreads();
+        if (i + 2 < nb) issue(i + 2);
+    }
+    acc.store(part + (cpart * SB + ccol) * RG);
+    __syncthreads();
+    if (fin) {
+        const int kn = min(SB, d.w - j * SB);
+#pragma unroll
+        for (int q = 0; q < FG; ++q) {
+            const int g = g0 + q;
+            if (g >= ng || ccol >= kn) break;
+            Cv x = part[ccol * RG + g];
+#pragma unroll
+            for (int p = 1; p < TPC; ++p) x += part[(p * SB + ccol) * RG + g];
+            work[d.first_col + j * SB + ccol + (long long)(rg + g) * A.ldw] = x;
+        }
+    }
+}
+
+}  // namespace uchol_dev

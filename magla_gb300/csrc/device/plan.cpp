@@ -442,6 +442,29 @@ Plan build_from_fronts(int n, int count, const int* first_column, const int* par
         for (int k0 = 0; k0 < P.sn[s].w; k0 += SB)
             P.inv_blocks.push_back({s, k0, std::min(SB, P.sn[s].w - k0), 0, 0, 1, (int)P.inv_blocks.size()});
     }
+    // inverse fronts: SB < w <= inv_cols; their off-diagonal inverse blocks, by diagonal i - j
+    std::vector<int> inv_ob(count, -1);
+    {
+        int max_nb = 0;
+        for (int s = 0; s < count; ++s) {
+            const int w = P.sn[s].w;
+            if (cfg.inv_cols <= 0 || w <= SB || w > cfg.inv_cols) continue;
+            const int nb = (w + SB - 1) / SB;
+            if (P.inv_off_blocks + (long long)nb * (nb - 1) / 2 > INT32_MAX) fail("too many inverse blocks");
+            inv_ob[s] = (int)P.inv_off_blocks;
+            P.inv_off_blocks += (long long)nb * (nb - 1) / 2;
+            max_nb = std::max(max_nb, nb);
+        }
+        for (int dg = 1; dg < max_nb; ++dg) {
+            const int b0 = (int)P.inv_tasks.size();
+            for (int s = 0; s < count; ++s) {
+                if (inv_ob[s] < 0) continue;
+                const int nb = (P.sn[s].w + SB - 1) / SB;
+                for (int i = dg; i < nb; ++i) P.inv_tasks.push_back({s, i, i - dg, inv_ob[s], 0, 0, first_blk[s]});
+            }
+            if ((int)P.inv_tasks.size() > b0) P.inv_launches.push_back({b0, (int)P.inv_tasks.size() - b0});
+        }
+    }
     constexpr int kGatherChunk = 512;   // rows per gather CTA (one CTA per chunk and right-hand side)
     // chunked per-front tasks: rows [r0, r1) of the front vector
     auto gather_tasks = [&](const std::vector<int>& fronts) {
@@ -503,23 +526,29 @@ Plan build_from_fronts(int n, int count, const int* first_column, const int* par
         P.progress_count += (int)bulk.size();
         return Lh;
     };
-    // fronts of one diagonal block go to the solo kernels, the others to the level kernels
-    auto split = [&](const std::vector<int>& fronts, std::vector<int>& multi) {
+    // fronts of one diagonal block go to the solo kernels, inverse fronts to their own kernels,
+    // the others to the level kernels
+    auto split = [&](const std::vector<int>& fronts, std::vector<int>& multi, std::vector<int>& inv) {
         SolveLaunch S{SolveLaunch::FwdSolo, (int)P.solve_tasks.size(), 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
         multi.clear();
+        inv.clear();
         for (int s : fronts) {
             if (P.sn[s].w <= SB) P.solve_tasks.push_back({s, 0, P.sn[s].w, 0, 0, 0, first_blk[s]});
+            else if (inv_ob[s] >= 0) inv.push_back(s);
             else multi.push_back(s);
         }
         S.count = (int)P.solve_tasks.size() - S.begin;
         return S;
     };
-    std::vector<int> multi;
+    auto simple = [&](SolveLaunch::Kind kind, int begin) {
+        return SolveLaunch{kind, begin, (int)P.solve_tasks.size() - begin, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    };
+    std::vector<int> multi, inv;
     for (int L = 0; L < P.levels; ++L) {
         const auto& fronts = at_level[L];
         auto g = gather_tasks(fronts);
         P.fwd_launches.push_back({SolveLaunch::FwdGather, g.first, g.second, 0, 0, 0, 0, 0, 0, 0, 0, 0});
-        SolveLaunch solo = split(fronts, multi);
+        SolveLaunch solo = split(fronts, multi, inv);
         if (solo.count > 0) P.fwd_launches.push_back(solo);
         // trailing rows of the single-block fronts, in chunks from w rounded down to 4
         int tb = (int)P.solve_tasks.size();
@@ -532,6 +561,24 @@ Plan build_from_fronts(int n, int count, const int* first_column, const int* par
         if ((int)P.solve_tasks.size() > tb)
             P.fwd_launches.push_back({SolveLaunch::FwdTail, tb, (int)P.solve_tasks.size() - tb, 0, 0, 0, 0, 0, 0, 0, 0, 0});
         if (!multi.empty()) P.fwd_launches.push_back(level_launch(SolveLaunch::FwdLevel, multi, true));
+        if (!inv.empty()) {
+            // y_1 per block row, then the trailing rows in chunks of SB - A rows (the tile copy starts
+            // at the chunk's first row rounded down to 16 bytes)
+            int b = (int)P.solve_tasks.size();
+            for (int s : inv) {
+                const int nb = (P.sn[s].w + SB - 1) / SB;
+                for (int i = 0; i < nb; ++i) P.solve_tasks.push_back({s, i, nb, inv_ob[s], 0, 0, first_blk[s]});
+            }
+            P.fwd_launches.push_back(simple(SolveLaunch::FwdInvDiag, b));
+            b = (int)P.solve_tasks.size();
+            const int height = SB - kTileAlignRows(cfg);
+            for (int s : inv) {
+                const SnDev& d = P.sn[s];
+                const int nb = (d.w + SB - 1) / SB;
+                for (int r = d.w; r < d.m; r += height) P.solve_tasks.push_back({s, 0, nb, r, std::min(d.m, r + height), 0, 0});
+            }
+            if ((int)P.solve_tasks.size() > b) P.fwd_launches.push_back(simple(SolveLaunch::FwdInvTail, b));
+        }
     }
     for (int L = P.levels - 1; L >= 0; --L) {
         const auto& fronts = at_level[L];
@@ -545,7 +592,7 @@ Plan build_from_fronts(int n, int count, const int* first_column, const int* par
         int slot = 0;
         for (int s : fronts) {
             const SnDev& d = P.sn[s];
-            if (d.m == d.w) continue;
+            if (d.m == d.w || inv_ob[s] >= 0) continue;
             const int nch = (d.m - d.w + kColRowsPlan - 1) / kColRowsPlan;
             for (int c = 0; c < d.w; c += 8) {
                 const int kn = std::min(8, d.w - c);
@@ -568,10 +615,33 @@ Plan build_from_fronts(int n, int count, const int* first_column, const int* par
             P.bwd_launches.push_back({SolveLaunch::BwdTailReduce, rb, (int)reduce.size(), 0, 0, 0, 0, 0, 0, 0, 0, 0});
         }
         P.bwd_partial_slots = std::max(P.bwd_partial_slots, slot);
-        SolveLaunch solo = split(fronts, multi);
+        SolveLaunch solo = split(fronts, multi, inv);
         solo.kind = SolveLaunch::BwdSolo;
         if (solo.count > 0) P.bwd_launches.push_back(solo);
         if (!multi.empty()) P.bwd_launches.push_back(level_launch(SolveLaunch::BwdLevel, multi, false));
+        if (!inv.empty()) {
+            // partial sums per (column block, chunk of kInvColRowsPlan trailing rows), then x_1 per
+            // block column, which adds its blocks' partial sums in chunk order
+            int b = (int)P.solve_tasks.size(), slots = 0;
+            std::vector<SolveBlockTask> diag_tasks;
+            for (int s : inv) {
+                const SnDev& d = P.sn[s];
+                const int nb = (d.w + SB - 1) / SB;
+                const int nq = (d.m - d.w + kInvColRowsPlan - 1) / kInvColRowsPlan;
+                for (int kb = 0; kb < nb; ++kb)
+                    for (int q = 0; q < nq; ++q) {
+                        const int r0 = d.w + q * kInvColRowsPlan;
+                        P.solve_tasks.push_back({s, kb, nb, r0, std::min(d.m, r0 + kInvColRowsPlan), 0, slots + kb * nq + q});
+                    }
+                for (int j = 0; j < nb; ++j) diag_tasks.push_back({s, j, nb, inv_ob[s], slots, nq, first_blk[s]});
+                slots += nb * nq;
+            }
+            if ((int)P.solve_tasks.size() > b) P.bwd_launches.push_back(simple(SolveLaunch::BwdInvCols, b));
+            P.inv_partial_slots = std::max(P.inv_partial_slots, slots);
+            b = (int)P.solve_tasks.size();
+            P.solve_tasks.insert(P.solve_tasks.end(), diag_tasks.begin(), diag_tasks.end());
+            P.bwd_launches.push_back(simple(SolveLaunch::BwdInvDiag, b));
+        }
     }
     return P;
 }

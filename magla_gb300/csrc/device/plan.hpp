@@ -15,6 +15,8 @@ namespace uchol_dev {
 constexpr int kSolveRowsPlan = 128;   // rows per panel-solve task (kSolveRows of the kernel)
 constexpr int kTailRowsPlan = 1024;  // trailing rows per forward tail task (kTailRows of the kernel)
 constexpr int kColRowsPlan = 2048;   // trailing rows per backward column-dot task (longer columns: partial sums)
+constexpr int kInvColRowsPlan = 1024;   // trailing rows per backward partial-sum task of an inverse front
+constexpr int kDefaultInvCols = 2048;   // widest front whose diagonal block is kept inverted for the solves
 constexpr int kSuperBlocks = 4;       // tensor-core path: outer blocks per super-block of the own-column updates
 constexpr int kDefaultMergeCols = 1024;   // widest device front made of a chain of supernodes (merge_chains)
 
@@ -25,6 +27,8 @@ struct PlanConfig {
     int tile = 64;            // SIMT tile edge (update kernels)
     bool tensor_core = false; // outer updates on tcgen05 from staged operands
     int solve_block = 64;     // column block of the triangular solves
+    int inv_cols = 0;         // > 0: fronts of solve_block < w <= inv_cols columns keep the whole inverse of their
+                              // unit-lower diagonal block, and their solves run without a block chain
     int merge_cols = 0;       // > 0: single-child chains of supernodes grouped into device fronts of at most
                               // this many columns (see merge_chains); 0: one device front per supernode
     double merge_fill = 0.05; // largest growth of the stored entries a grouping may cost
@@ -58,7 +62,10 @@ struct Launch {
 };
 
 struct SolveLaunch {
-    enum Kind : int { FwdGather, FwdSolo, FwdLevel, BwdGather, BwdTail, BwdSolo, BwdLevel, FwdTail, BwdTailReduce } kind;
+    enum Kind : int {
+        FwdGather, FwdSolo, FwdLevel, BwdGather, BwdTail, BwdSolo, BwdLevel, FwdTail, BwdTailReduce,
+        FwdInvDiag, FwdInvTail, BwdInvCols, BwdInvDiag, KindCount
+    } kind;
     int begin, count;   // tasks; level launches: the chains (one per front)
     int steps;          // level launches: most diagonal blocks of one front of the level
     int bulk_begin, bulk_count;   // level launches: the bulk chunks
@@ -67,6 +74,22 @@ struct SolveLaunch {
     int long_chains;                   // level launches: fronts of three or more diagonal blocks
     int ndiag;                         // level launches: bulk chunks [0, ndiag) are diagonal blocks
     long long diag_work;               // level launches: chunk updates of those
+};
+
+// Inverse fronts (cfg.inv_cols): the off-diagonal blocks (i, j), i > j, of the
+// inverse of the unit-lower diagonal block, SB x SB column-major each, front s's
+// at block index ob_s + i (i - 1) / 2 + j of the off-diagonal arena.  Tasks:
+//   inversion            {s, i, j, ob_s, -, -, blk}: block (i, j) from the blocks
+//                        (k, j), j <= k < i (launched by diagonal i - j);
+//   FwdInvDiag           {s, i, nb, ob_s, -, -, blk}: y_i = sum_{j <= i} Linv(i, j) f_j;
+//   FwdInvTail           {s, -, nb, r0, r1, -, -}: f[r0, r1) -= L[r0:r1, 0:w] y;
+//   BwdInvCols           {s, kb, nb, r0, r1, -, slot}: partial sums of L[r0:r1, block kb]^T g
+//                        into partial slot `slot`;
+//   BwdInvDiag           {s, j, nb, ob_s, slot0, nq, blk}: g_i -= its nq partial slots
+//                        slot0 + i nq + (0 .. nq-1), then x_j = sum_{i >= j} Linv(i, j)^T g_i.
+// blk is the diagonal-inverse index of the front's block 0.
+struct InvLaunch {
+    int begin, count;   // inversion tasks of one diagonal i - j
 };
 
 // Solve task of supernode s.  Gathers: rows [r0, r1) of the front vector.
@@ -136,6 +159,10 @@ struct Plan {
     std::vector<SolveBlockTask> solve_tasks;
     std::vector<SolveBlockTask> inv_blocks;    // every diagonal block, for the inversion after a factorisation
     std::vector<SolveLaunch> fwd_launches, bwd_launches;
+    std::vector<SolveBlockTask> inv_tasks;     // inverse fronts: off-diagonal inverse blocks, by diagonal
+    std::vector<InvLaunch> inv_launches;
+    long long inv_off_blocks = 0;              // blocks of the off-diagonal inverse arena
+    int inv_partial_slots = 0;                 // most BwdInvCols partial slots of one launch (SB x nrhs each)
     int progress_count = 0;                    // progress counters of all level launches
     int bwd_partial_slots = 0;                 // most backward column-dot partial slots of one launch (8 x nrhs each)
 };

@@ -58,6 +58,7 @@ class UtduSolverOptions:
         self.BlockWidth = 0
         self.SmallFrontBuckets = 0   # bit b: fronts of 32b < m <= 32(b+1) rows go whole to one CTA (0 = 0x7)
         self.ChainMergeWidth = 0     # widest device front grouped from a chain of supernodes (0 = 1024, < 0 = off)
+        self.InverseBlockWidth = 0   # widest front whose diagonal block is kept inverted for the solves (0 = 2048, < 0 = off)
         self.RefinementTolerance = 1e-12
         self.RefinementMaxIterations = 50
         for k, v in kw.items():
@@ -82,6 +83,7 @@ class UtduSolverOptions:
         o.block_width = int(self.BlockWidth)
         o.small_front_buckets = int(self.SmallFrontBuckets)
         o.chain_merge_width = int(self.ChainMergeWidth)
+        o.inverse_block_width = int(self.InverseBlockWidth)
         return o
 
 
