@@ -104,12 +104,38 @@ __global__ void __launch_bounds__(256) k_inv_offdiag(const SolveBlockTask* __res
 template <class T, int SB>
 constexpr size_t inv_offdiag_smem() { return (size_t)2 * SB * SB * sizeof(T); }
 
-// Shared memory of the inverse-front solve kernels: two SB x SB tile stages, a
-// right-hand block (SB rows x RG, stride RS) and the partial sums.
+// Shared memory of the inverse-front solve kernels: two SB x SB tile stages, two
+// right-hand blocks (SB rows x RG, stride RS) and the partial sums.
 template <class T, class Cv, int SB, int RG>
 constexpr size_t inv_solve_smem() {
     return (size_t)2 * SB * SB * sizeof(T) + LevelRhs<Cv, SB, RG>::bytes + kLevelSmemSlack;
 }
+
+// Register prefetch of an SB x RG right-hand block: thread t holds elements t + 256 q;
+// fetch() issues the global loads of the next block before the current tile's products,
+// commit() stores them into shared memory (row c at c RS, right-hand side g at + g) after.
+template <class Cv, int SB, int RG>
+struct RhsPrefetch {
+    static constexpr int PQ = (SB * RG + 255) / 256;
+    static constexpr int RS = LevelRhs<Cv, SB, RG>::RS;
+    Cv v[PQ];
+    // f(c, g) -> the value of row c, right-hand side g (zero where absent)
+    template <class F>
+    __device__ __forceinline__ void fetch(F&& f) {
+#pragma unroll
+        for (int q = 0; q < PQ; ++q) {
+            const int e = (int)threadIdx.x + 256 * q, g = e / SB, c = e - g * SB;
+            v[q] = e < SB * RG ? f(c, g) : Cv(0);
+        }
+    }
+    __device__ __forceinline__ void commit(Cv* buf) const {
+#pragma unroll
+        for (int q = 0; q < PQ; ++q) {
+            const int e = (int)threadIdx.x + 256 * q, g = e / SB, c = e - g * SB;
+            if (e < SB * RG) buf[c * RS + g] = v[q];
+        }
+    }
+};
 
 // Forward y_i = sum_{j <= i} Linv(i, j) f_j for right-hand sides [RG blockIdx.y, +RG);
 // writes y_i (front vector yv) and y_i / D (work).  Thread (row, pid) sums columns
@@ -126,8 +152,9 @@ __global__ void __launch_bounds__(256, 1) k_fwd_inv_diag(const SolveBlockTask* _
     unsigned char* sm = blk_smem + ((1024u - (smem_addr(blk_smem) & 1023u)) & 1023u);
     Cv* const stage0 = reinterpret_cast<Cv*>(sm);        // two Linv tile stages
     auto stage = [&](int k) { return stage0 + k * SB * SB; };
-    Cv* fb = stage0 + 2 * SB * SB;                       // f_j: SB rows x RG
-    Cv* part = fb + 2 * SB * RS;
+    Cv* const fb0 = stage0 + 2 * SB * SB;                // two blocks f_j: SB rows x RG
+    auto fbuf = [&](int k) { return fb0 + k * SB * RS; };
+    Cv* part = fb0 + 2 * SB * RS;
     __shared__ unsigned long long bar[2];
     const SolveBlockTask tk = tasks[blockIdx.x];
     const SnDev d = A.sn[tk.s];
@@ -141,7 +168,6 @@ __global__ void __launch_bounds__(256, 1) k_fwd_inv_diag(const SolveBlockTask* _
         bar_init(&bar[0]);
         bar_init(&bar[1]);
     }
-    __syncthreads();
     constexpr unsigned kTileBytes = SB * SB * sizeof(Cv);
     auto issue = [&](int jj) {
         if (tid == 0) {
@@ -150,20 +176,28 @@ __global__ void __launch_bounds__(256, 1) k_fwd_inv_diag(const SolveBlockTask* _
             bulk_g2s(stage(jj & 1), inv_block<Cv, SB>(linv, linv_off, blk, ob, i, jj), kTileBytes, &bar[jj & 1]);
         }
     };
+    // f_j, zero past the front's columns and the group's right-hand sides
+    RhsPrefetch<Cv, SB, RG> pf;
+    auto fetch = [&](int j) {
+        pf.fetch([&](int c, int g) {
+            const int col = j * SB + c;
+            return (g < ng && col < d.w) ? fv[fo + (long long)(rg + g) * A.fv_stride + col] : Cv(0);
+        });
+    };
+    fetch(0);
+    __syncthreads();   // barriers initialised
     issue(0);
     if (i >= 1) issue(1);
+    pf.commit(fbuf(0));
+    if (i >= 1) fetch(1);
     RhsAcc<Cv, RG> acc;
     acc.zero();
     unsigned phase = 0;
     for (int j = 0; j <= i; ++j) {
-        // f_j, zero past the front's columns and the group's right-hand sides
-        for (int e = tid; e < SB * RG; e += blockDim.x) {
-            const int g = e / SB, c = e - g * SB, col = j * SB + c;
-            fb[c * RS + g] = (g < ng && col < d.w) ? fv[fo + (long long)(rg + g) * A.fv_stride + col] : Cv(0);
-        }
         if (!__syncthreads_and(bar_wait(&bar[j & 1], (phase >> (j & 1)) & 1u, status))) return;
         phase ^= 1u << (j & 1);
         const Cv* tile = stage(j & 1);
+        const Cv* fb = fbuf(j & 1);
 #pragma unroll 2
         for (int u0 = 0; u0 < CPT; u0 += 4)
 #pragma unroll
@@ -171,7 +205,9 @@ __global__ void __launch_bounds__(256, 1) k_fwd_inv_diag(const SolveBlockTask* _
                 const int c = pid * CPT + u0 + q;
                 acc.add(q, tile[row + c * SB], fb + c * RS);
             }
-        __syncthreads();   // the stage and fb are free again
+        if (j + 1 <= i) pf.commit(fbuf((j + 1) & 1));
+        if (j + 2 <= i) fetch(j + 2);
+        __syncthreads();   // the stage is free again
         if (j + 2 <= i) issue(j + 2);
     }
     acc.store(part + (pid * SB + row) * RG);
@@ -205,8 +241,9 @@ __global__ void __launch_bounds__(256, 1) k_fwd_inv_tail(const SolveBlockTask* _
     unsigned char* sm = blk_smem + ((1024u - (smem_addr(blk_smem) & 1023u)) & 1023u);
     T* const stage0 = reinterpret_cast<T*>(sm);          // two tile stages
     auto stage = [&](int k) { return stage0 + k * SB * SB; };
-    Cv* yb = reinterpret_cast<Cv*>(stage0 + 2 * SB * SB);
-    Cv* part = yb + 2 * SB * RS;
+    Cv* const yb0 = reinterpret_cast<Cv*>(stage0 + 2 * SB * SB);   // two blocks y_kb: SB rows x RG
+    auto ybuf = [&](int k) { return yb0 + k * SB * RS; };
+    Cv* part = yb0 + 2 * SB * RS;
     __shared__ unsigned long long bar[2];
     const SolveBlockTask tk = tasks[blockIdx.x];
     const SnDev d = A.sn[tk.s];
@@ -222,23 +259,29 @@ __global__ void __launch_bounds__(256, 1) k_fwd_inv_tail(const SolveBlockTask* _
     }
     __syncthreads();
     unsigned phase = 0;
+    RhsPrefetch<Cv, SB, RG> pf;
     for (int rg = 0; rg < A.nrhs; rg += RG) {
         const int ng = min(RG, A.nrhs - rg);
+        auto fetch = [&](int kb) {
+            const int kn = min(SB, d.w - kb * SB);
+            pf.fetch([&](int c, int g) {
+                return (g < ng && c < kn) ? yv[fo + (long long)(rg + g) * A.fv_stride + kb * SB + c] : Cv(0);
+            });
+        };
+        fetch(0);
         if (tid == 0) {
             start_bulk_tile<T, SB>(stage(0), maps + tk.s, ra, 0, &bar[0]);
             if (nb > 1) start_bulk_tile<T, SB>(stage(1), maps + tk.s, ra, SB, &bar[1]);
         }
+        pf.commit(ybuf(0));
+        if (nb > 1) fetch(1);
         RhsAcc<Cv, RG> acc;
         acc.zero();
         for (int kb = 0; kb < nb; ++kb) {
-            const int kn = min(SB, d.w - kb * SB);
-            for (int e = tid; e < SB * RG; e += blockDim.x) {
-                const int g = e / SB, c = e - g * SB;
-                yb[c * RS + g] = (g < ng && c < kn) ? yv[fo + (long long)(rg + g) * A.fv_stride + kb * SB + c] : Cv(0);
-            }
             if (!__syncthreads_and(bar_wait(&bar[kb & 1], (phase >> (kb & 1)) & 1u, status))) return;
             phase ^= 1u << (kb & 1);
             const T* tile = stage(kb & 1);
+            const Cv* yb = ybuf(kb & 1);
 #pragma unroll 2
             for (int u0 = 0; u0 < CPT; u0 += 4)
 #pragma unroll
@@ -246,7 +289,9 @@ __global__ void __launch_bounds__(256, 1) k_fwd_inv_tail(const SolveBlockTask* _
                     const int c = pid * CPT + u0 + q;
                     acc.add(q, (Cv)tile[trow + c * SB], yb + c * RS);
                 }
-            __syncthreads();   // the stage and yb are free again
+            if (kb + 1 < nb) pf.commit(ybuf((kb + 1) & 1));
+            if (kb + 2 < nb) fetch(kb + 2);
+            __syncthreads();   // the stage is free again
             if (tid == 0 && kb + 2 < nb) start_bulk_tile<T, SB>(stage(kb & 1), maps + tk.s, ra, (kb + 2) * SB, &bar[kb & 1]);
         }
         acc.store(part + (pid * SB + row) * RG);
@@ -281,8 +326,9 @@ __global__ void __launch_bounds__(256, 1) k_bwd_inv_cols(const SolveBlockTask* _
     unsigned char* sm = blk_smem + ((1024u - (smem_addr(blk_smem) & 1023u)) & 1023u);
     T* const stage0 = reinterpret_cast<T*>(sm);          // two tile stages
     auto stage = [&](int k) { return stage0 + k * SB * SB; };
-    Cv* xb = reinterpret_cast<Cv*>(stage0 + 2 * SB * SB);
-    Cv* part = xb + 2 * SB * RS;
+    Cv* const xb0 = reinterpret_cast<Cv*>(stage0 + 2 * SB * SB);   // two blocks of g: SB rows x RG
+    auto xbuf = [&](int k) { return xb0 + k * SB * RS; };
+    Cv* part = xb0 + 2 * SB * RS;
     __shared__ unsigned long long bar[2];
     const SolveBlockTask tk = tasks[blockIdx.x];
     const int kb = tk.k0, r0 = tk.r0, r1 = tk.r1, ra = r0 & ~(kAlign - 1);
@@ -297,24 +343,30 @@ __global__ void __launch_bounds__(256, 1) k_bwd_inv_cols(const SolveBlockTask* _
     }
     __syncthreads();
     unsigned phase = 0;
+    RhsPrefetch<Cv, SB, RG> pf;
     for (int rg = 0; rg < A.nrhs; rg += RG) {
         const int ng = min(RG, A.nrhs - rg);
+        auto fetch = [&](int t) {
+            const int tr = ra + t * SB;
+            pf.fetch([&](int r, int g) {
+                const int gr = tr + r;
+                return (g < ng && gr >= r0 && gr < r1) ? fv[fo + (long long)(rg + g) * A.fv_stride + gr] : Cv(0);
+            });
+        };
+        fetch(0);
         if (tid == 0) {
             start_bulk_tile<T, SB>(stage(0), maps + tk.s, ra, kb * SB, &bar[0]);
             if (ntile > 1) start_bulk_tile<T, SB>(stage(1), maps + tk.s, ra + SB, kb * SB, &bar[1]);
         }
+        pf.commit(xbuf(0));
+        if (ntile > 1) fetch(1);
         RhsAcc<Cv, RG> acc;
         acc.zero();
         for (int t = 0; t < ntile; ++t) {
-            const int tr = ra + t * SB;
-            for (int e = tid; e < SB * RG; e += blockDim.x) {
-                const int g = e / SB, r = e - g * SB, gr = tr + r;
-                xb[r * RS + g] =
-                    (g < ng && gr >= r0 && gr < r1) ? fv[fo + (long long)(rg + g) * A.fv_stride + gr] : Cv(0);
-            }
             if (!__syncthreads_and(bar_wait(&bar[t & 1], (phase >> (t & 1)) & 1u, status))) return;
             phase ^= 1u << (t & 1);
             const T* tile = stage(t & 1);
+            const Cv* xb = xbuf(t & 1);
 #pragma unroll 2
             for (int u0 = 0; u0 < RPT; u0 += 4)
 #pragma unroll
@@ -322,6 +374,8 @@ __global__ void __launch_bounds__(256, 1) k_bwd_inv_cols(const SolveBlockTask* _
                     const int r = cpart * RPT + ((u0 + q + ccol) & (RPT - 1));
                     acc.add(q, (Cv)tile[r + ccol * SB], xb + r * RS);
                 }
+            if (t + 1 < ntile) pf.commit(xbuf((t + 1) & 1));
+            if (t + 2 < ntile) fetch(t + 2);
             __syncthreads();
             if (tid == 0 && t + 2 < ntile) start_bulk_tile<T, SB>(stage(t & 1), maps + tk.s, ra + (t + 2) * SB, kb * SB, &bar[t & 1]);
         }
@@ -356,8 +410,9 @@ __global__ void __launch_bounds__(256, 1) k_bwd_inv_diag(const SolveBlockTask* _
     unsigned char* sm = blk_smem + ((1024u - (smem_addr(blk_smem) & 1023u)) & 1023u);
     Cv* const stage0 = reinterpret_cast<Cv*>(sm);        // two Linv tile stages
     auto stage = [&](int k) { return stage0 + k * SB * SB; };
-    Cv* gb = stage0 + 2 * SB * SB;
-    Cv* part = gb + 2 * SB * RS;
+    Cv* const gb0 = stage0 + 2 * SB * SB;                // two blocks g_i: SB rows x RG
+    auto gbuf = [&](int k) { return gb0 + k * SB * RS; };
+    Cv* part = gb0 + 2 * SB * RS;
     __shared__ unsigned long long bar[2];
     const SolveBlockTask tk = tasks[blockIdx.x];
     const SnDev d = A.sn[tk.s];
@@ -371,7 +426,6 @@ __global__ void __launch_bounds__(256, 1) k_bwd_inv_diag(const SolveBlockTask* _
         bar_init(&bar[0]);
         bar_init(&bar[1]);
     }
-    __syncthreads();
     constexpr unsigned kTileBytes = SB * SB * sizeof(Cv);
     auto issue = [&](int ii) {
         if (tid == 0) {
@@ -381,26 +435,34 @@ __global__ void __launch_bounds__(256, 1) k_bwd_inv_diag(const SolveBlockTask* _
             bulk_g2s(stage(st), inv_block<Cv, SB>(linv, linv_off, blk, ob, ii, j), kTileBytes, &bar[st]);
         }
     };
-    issue(j);
-    if (j + 1 < nb) issue(j + 1);
-    RhsAcc<Cv, RG> acc;
-    acc.zero();
-    unsigned phase = 0;
-    for (int i = j; i < nb; ++i) {
-        const int st = (i - j) & 1;
-        for (int e = tid; e < SB * RG; e += blockDim.x) {
-            const int g = e / SB, c = e - g * SB, col = i * SB + c;
+    RhsPrefetch<Cv, SB, RG> pf;
+    auto fetch = [&](int i) {
+        pf.fetch([&](int c, int g) {
+            const int col = i * SB + c;
             Cv v = Cv(0);
             if (g < ng && col < d.w) {
                 v = fv[fo + (long long)(rg + g) * A.fv_stride + col];
                 const Cv* pp = partial + ((long long)(slot0 + i * nq) * A.nrhs + rg + g) * SB + c;
                 for (int q = 0; q < nq; ++q) v -= pp[(long long)q * A.nrhs * SB];
             }
-            gb[c * RS + g] = v;
-        }
+            return v;
+        });
+    };
+    fetch(j);
+    __syncthreads();   // barriers initialised
+    issue(j);
+    if (j + 1 < nb) issue(j + 1);
+    pf.commit(gbuf(0));
+    if (j + 1 < nb) fetch(j + 1);
+    RhsAcc<Cv, RG> acc;
+    acc.zero();
+    unsigned phase = 0;
+    for (int i = j; i < nb; ++i) {
+        const int st = (i - j) & 1;
         if (!__syncthreads_and(bar_wait(&bar[st], (phase >> st) & 1u, status))) return;
         phase ^= 1u << st;
         const Cv* tile = stage(st);
+        const Cv* gb = gbuf(st);
 #pragma unroll 2
         for (int u0 = 0; u0 < RPT; u0 += 4)
 #pragma unroll
@@ -408,6 +470,8 @@ __global__ void __launch_bounds__(256, 1) k_bwd_inv_diag(const SolveBlockTask* _
                 const int c = cpart * RPT + ((u0 + q + ccol) & (RPT - 1));
                 acc.add(q, tile[c + ccol * SB], gb + c * RS);
             }
+        if (i + 1 < nb) pf.commit(gbuf(st ^ 1));
+        if (i + 2 < nb) fetch(i + 2);
         __syncthreads();
         if (i + 2 < nb) issue(i + 2);
     }
