@@ -166,7 +166,7 @@ int uchol_solve_refined_device(uchol_factor f, int n, int nrhs, const double* d_
 int uchol_residual_norms(uchol_factor f, int n, int nrhs, const double* b, int ldb, const double* x, int ldx,
                          double* out_norms);
 
-#define UCHOL_SOLVE_KINDS 13
+#define UCHOL_SOLVE_KINDS 14
 
 /* Device-time of the last call on the handle's stream, per phase. */
 typedef struct {
@@ -180,8 +180,8 @@ typedef struct {
      * gather, 1 forward single-block fronts, 2 forward level kernels, 3 backward gather,
      * 4 backward column dots, 5 backward single-block fronts, 6 backward level kernels,
      * 7 forward trailing rows of single-block fronts, 8 backward partial-sum reductions,
-     * 9-12 inverse fronts: forward diagonal, forward trailing rows, backward partial sums,
-     * backward diagonal. */
+     * 9-13 inverse fronts: forward diagonal, forward trailing rows, backward partial sums,
+     * backward diagonal, backward partial-sum reductions. */
     double solve_kind_ms[UCHOL_SOLVE_KINDS];
     double solve_total_ms;       /* sum over the solve's launches */
     int solve_launches;

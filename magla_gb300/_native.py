@@ -93,12 +93,13 @@ class PhaseTimes(C.Structure):
     _fields_ = [("pivot_block_ms", C.c_double), ("extend_add_ms", C.c_double), ("small_fronts_ms", C.c_double),
                 ("panel_ms", C.c_double), ("schur_ms", C.c_double), ("total_ms", C.c_double),
                 ("launches", C.c_int), ("schur_tensor_flops", C.c_double), ("schur_tensor_ms", C.c_double),
-                ("schur_tensor_launches", C.c_int), ("solve_kind_ms", C.c_double * 13), ("solve_total_ms", C.c_double),
+                ("schur_tensor_launches", C.c_int), ("solve_kind_ms", C.c_double * 14), ("solve_total_ms", C.c_double),
                 ("solve_launches", C.c_int)]
 
 # launch kinds of PhaseTimes.solve_kind_ms
 SOLVE_KINDS = ("fwd_gather", "fwd_solo", "fwd_level", "bwd_gather", "bwd_cols", "bwd_solo", "bwd_level", "fwd_tail",
-               "bwd_cols_reduce", "fwd_inv_diag", "fwd_inv_tail", "bwd_inv_cols", "bwd_inv_diag")
+               "bwd_cols_reduce", "fwd_inv_diag", "fwd_inv_tail", "bwd_inv_cols", "bwd_inv_diag",
+               "bwd_inv_reduce")
 
 
 HOST_SYMBOLS = {

@@ -199,7 +199,7 @@ struct uchol_factor_s {
     DBuf inv_partial;                   // inverse fronts: backward partial sums (solve workspace)
     DBuf minv;                          // mixed path: per outer block X^T, D, D^{-1} of each diagonal block
     DBuf solve_flags;                   // per diagonal block: forward and backward "solution published" flags
-    DBuf solve_maps;                    // per supernode: tensor map of the diagonal region of its panel
+    DBuf solve_maps;                    // per front: tensor maps of its panel, boxes SB x SB, SB x SB/2, SB/2 x SB
     DBuf solve_status;                  // nonzero once a bounded wait of a solve expired
     int coop_fwd = 0, coop_bwd = 0;     // resident CTAs of the level solve kernels (whole device)
     int ws_nrhs = 0;
@@ -813,8 +813,8 @@ void run_solve(uchol_factor_s* F, int nrhs, Cv* work, Cv* fv, Cv* fv2, cudaStrea
             k_fwd_inv_diag<T, Cv, SB, RGD><<<dim3(L.count, (nrhs + RGD - 1) / RGD), 256, inv_solve_smem<T, Cv, SB, RGD>(), st>>>(
                 tasks + L.begin, A, linv, F->linv_off.as<Cv>(), fv, fv2, diag, work, status);
         } else if (L.kind == SolveLaunch::FwdInvTail) {
-            k_fwd_inv_tail<T, Cv, SB, RG><<<L.count, 256, inv_solve_smem<T, Cv, SB, RG>(), st>>>(
-                tasks + L.begin, A, F->solve_maps.as<CUtensorMap>(), fv2, fv, status);
+            k_fwd_inv_tail<T, Cv, SB, RG><<<L.count, 256, inv_tail_smem<T, Cv, SB, RG, false>(), st>>>(
+                tasks + L.begin, A, F->solve_maps.as<CUtensorMap>() + P.count, fv2, fv, status);
         } else if (L.kind == SolveLaunch::FwdTail) {
             if (nrhs == 1)
                 k_fwd_tail<T, Cv, SB, 1><<<L.count, kTailRows / 4, 0, st>>>(tasks + L.begin, A, panel, fv2, fv);
@@ -837,11 +837,14 @@ void run_solve(uchol_factor_s* F, int nrhs, Cv* work, Cv* fv, Cv* fv2, cudaStrea
         } else if (L.kind == SolveLaunch::BwdTailReduce) {
             k_bwd_cols_reduce<Cv><<<L.count, 128, 0, st>>>(tasks + L.begin, A, F->bwd_partial.as<Cv>(), fv);
         } else if (L.kind == SolveLaunch::BwdInvCols) {
-            k_bwd_inv_cols<T, Cv, SB, RG><<<L.count, 256, inv_solve_smem<T, Cv, SB, RG>(), st>>>(
-                tasks + L.begin, A, F->solve_maps.as<CUtensorMap>(), fv, F->inv_partial.as<Cv>(), status);
+            k_bwd_inv_cols<T, Cv, SB, RG><<<L.count, 256, inv_tail_smem<T, Cv, SB, RG, true>(), st>>>(
+                tasks + L.begin, A, F->solve_maps.as<CUtensorMap>() + 2 * P.count, fv, F->inv_partial.as<Cv>(), status);
+        } else if (L.kind == SolveLaunch::BwdInvReduce) {
+            k_bwd_inv_reduce<Cv, SB><<<dim3(L.count, std::min(nrhs, 65535)), SB, 0, st>>>(tasks + L.begin, A, fv,
+                                                                                        F->inv_partial.as<Cv>());
         } else if (L.kind == SolveLaunch::BwdInvDiag) {
             k_bwd_inv_diag<T, Cv, SB, RGD><<<dim3(L.count, (nrhs + RGD - 1) / RGD), 256, inv_solve_smem<T, Cv, SB, RGD>(), st>>>(
-                tasks + L.begin, A, linv, F->linv_off.as<Cv>(), fv, F->inv_partial.as<Cv>(), work, status);
+                tasks + L.begin, A, linv, F->linv_off.as<Cv>(), fv, work, status);
         } else if (L.kind == SolveLaunch::BwdSolo) {
             k_bwd_solo<Cv, SB><<<L.count, 256, 0, st>>>(tasks + L.begin, A, linv, fv, fv2, work);
         } else {
@@ -898,33 +901,40 @@ void launch_solve_graph(uchol_factor_s* F, int nrhs, Cv* work, cudaStream_t st) 
         CK(cudaFuncSetAttribute(k_bwd_inv_diag<T, Cv, SB, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)inv_solve_smem<T, Cv, SB, 4>()));
         CK(cudaFuncSetAttribute(k_fwd_inv_tail<T, Cv, SB, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)inv_solve_smem<T, Cv, SB, 1>()));
+                                (int)inv_tail_smem<T, Cv, SB, 1, false>()));
         CK(cudaFuncSetAttribute(k_fwd_inv_tail<T, Cv, SB, kSolveRhsGroup>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)inv_solve_smem<T, Cv, SB, kSolveRhsGroup>()));
+                                (int)inv_tail_smem<T, Cv, SB, kSolveRhsGroup, false>()));
         CK(cudaFuncSetAttribute(k_bwd_inv_cols<T, Cv, SB, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)inv_solve_smem<T, Cv, SB, 1>()));
+                                (int)inv_tail_smem<T, Cv, SB, 1, true>()));
         CK(cudaFuncSetAttribute(k_bwd_inv_cols<T, Cv, SB, kSolveRhsGroup>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)inv_solve_smem<T, Cv, SB, kSolveRhsGroup>()));
+                                (int)inv_tail_smem<T, Cv, SB, kSolveRhsGroup, true>()));
         if (F->coop_fwd < 2 || F->coop_bwd < 2) throw Error(UCHOL_CUDA_ERROR, "the level solve kernels do not fit");
         if (!F->solve_maps.p) {
-            // tile copies of the level solves: each front's panel (m x w)
+            // tile copies of the solves: each front's panel (m x w), in boxes of SB x SB (level
+            // kernels), SB x SB/2 and SB/2 x SB (half tiles of the inverse-front kernels)
             const Plan& P = F->dp->plan;
-            std::vector<CUtensorMap> maps(std::max(1, (int)P.sn.size()));
+            const size_t nf = P.sn.size();
+            std::vector<CUtensorMap> maps(std::max<size_t>(1, 3 * nf));
             std::memset(maps.data(), 0, maps.size() * sizeof(CUtensorMap));
             const size_t es = sizeof(T);
-            for (size_t s2 = 0; s2 < P.sn.size(); ++s2) {
-                const SnDev& d = P.sn[s2];   // every front: its trailing rows are bulk tiles too
-                cuuint64_t dims[2] = {(cuuint64_t)d.m, (cuuint64_t)d.w};
-                cuuint64_t strides[1] = {(cuuint64_t)d.ldp * es};
-                cuuint32_t box[2] = {(cuuint32_t)SB, (cuuint32_t)SB};
-                cuuint32_t estr[2] = {1, 1};
-                CUresult r = tensor_map_encoder()(&maps[s2], es == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
-                                                  2, (char*)F->panel.p + (size_t)d.panel_off * es, dims, strides, box,
-                                                  estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                                                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-                if (r != CUDA_SUCCESS)
-                    throw Error(UCHOL_CUDA_ERROR, "cuTensorMapEncodeTiled failed for a solve tile map: " + std::to_string((int)r));
-            }
+            const cuuint32_t boxes[3][2] = {{(cuuint32_t)SB, (cuuint32_t)SB}, {(cuuint32_t)SB, (cuuint32_t)(SB / 2)},
+                                            {(cuuint32_t)(SB / 2), (cuuint32_t)SB}};
+            for (int kind = 0; kind < 3; ++kind)
+                for (size_t s2 = 0; s2 < nf; ++s2) {
+                    const SnDev& d = P.sn[s2];   // every front: its trailing rows are bulk tiles too
+                    cuuint64_t dims[2] = {(cuuint64_t)d.m, (cuuint64_t)d.w};
+                    cuuint64_t strides[1] = {(cuuint64_t)d.ldp * es};
+                    cuuint32_t box[2] = {boxes[kind][0], boxes[kind][1]};
+                    cuuint32_t estr[2] = {1, 1};
+                    CUresult r = tensor_map_encoder()(&maps[kind * nf + s2],
+                                                      es == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
+                                                      2, (char*)F->panel.p + (size_t)d.panel_off * es, dims, strides, box,
+                                                      estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                    if (r != CUDA_SUCCESS)
+                        throw Error(UCHOL_CUDA_ERROR,
+                                    "cuTensorMapEncodeTiled failed for a solve tile map: " + std::to_string((int)r));
+                }
             F->solve_maps.upload(maps, st, "solve tile maps");
             CK(cudaStreamSynchronize(st));
         }

@@ -4,8 +4,9 @@
 //   y_1 = Linv_11 f_1                  (k_fwd_inv_diag: one CTA per block row),
 //   f_2 -= L_21 y_1                    (k_fwd_inv_tail: one CTA per chunk of trailing rows);
 // backward:
-//   g_1 -= L_21^T g_2                  (k_bwd_inv_cols: partial sums per chunk of rows),
-//   x_1 = Linv_11^T g_1                (k_bwd_inv_diag: adds the partial sums in order).
+//   g_1 -= L_21^T g_2                  (k_bwd_inv_cols: partial sums per chunk of rows;
+//                                       k_bwd_inv_reduce adds them in chunk order),
+//   x_1 = Linv_11^T g_1                (k_bwd_inv_diag: one CTA per block column).
 // The algebra is the reference's supernodal substitution
 // (CAESolvers/UCHOL/UtduNumericFactorization.cs:139-207) with the triangular solve of
 // the diagonal block written as a product with its inverse; the result differs only
@@ -228,30 +229,104 @@ __global__ void __launch_bounds__(256, 1) k_fwd_inv_diag(const SolveBlockTask* _
     }
 }
 
-// Forward trailing rows [r0, r1) of an inverse front: f -= L[r0:r1, 0:w] y, tile by
-// tile (tensor-map copies, two stages); the tiles start at r0 rounded down to 16 bytes.
+// Register tiles of the trailing-row kernels.  A thread accumulates RT rows (forward) or
+// RT columns (backward) by GT right-hand sides; RT elements are 16 bytes, so the forward
+// kernel reads them as one vector.  NG groups of RT rows (columns) cover SB, NH groups of
+// GT cover the RG right-hand sides, and the NS remaining thread groups split the half
+// tile's columns (forward) or rows (backward); their partial sums are added at the end.
+template <class Cv, int SB, int RG>
+struct TailTiles {
+    static constexpr int RT = 16 / (int)sizeof(Cv);
+    static constexpr int GT = RG < 8 ? RG : 8;
+    static constexpr int NH = RG / GT;
+    static constexpr int NG = SB / RT;
+    static constexpr int NS = 256 / (NG * NH);
+    static constexpr int RS = LevelRhs<Cv, SB, RG>::RS;   // row stride of the right-hand blocks
+    static_assert(NG * NH * NS == 256 && RG % GT == 0, "thread tiles must cover the CTA");
+};
+
+// Shared memory of the trailing-row kernels: two half-tile stages, the transposed half tile
+// (backward only; rows of SB + 1 so that the transpose and the column reads are free of
+// bank conflicts), two right-hand blocks of SB/2 rows; the partial sums (NS x SB x RG) reuse
+// the stages after the last tile.  Two CTAs fit on an SM.
+template <class T, class Cv, int SB, int RG, bool kTransposed>
+constexpr size_t inv_tail_smem() {
+    return (size_t)SB * SB * sizeof(T) + (kTransposed ? (size_t)(SB / 2) * (SB + 1) * sizeof(T) : 0) +
+           (size_t)2 * (SB / 2) * TailTiles<Cv, SB, RG>::RS * sizeof(Cv) + kLevelSmemSlack;
+}
+static_assert((size_t)TailTiles<float, 128, 16>::NS * 128 * 16 * sizeof(float) <= (size_t)128 * 128 * sizeof(float),
+              "the partial sums fit in the tile stages");
+static_assert((size_t)TailTiles<double, 64, 16>::NS * 64 * 16 * sizeof(double) <= (size_t)64 * 64 * sizeof(double),
+              "the partial sums fit in the tile stages");
+
+// Starts a tensor-map tile copy of `bytes` bytes at (x, y) into dst, completing on bar (one thread).
+__device__ __forceinline__ void start_box_tile(void* dst, const CUtensorMap* map, int x, int y, unsigned bytes,
+                                               unsigned long long* bar) {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    bar_expect(bar, bytes);
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+            smem_addr(dst)),
+        "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(smem_addr(bar))
+        : "memory");
+}
+
+// RT consecutive elements of shared memory (16-byte aligned), widened.
+__device__ __forceinline__ void lds_vec(const float* p, float (&v)[4]) {
+    const float4 q = *reinterpret_cast<const float4*>(p);
+    v[0] = q.x;
+    v[1] = q.y;
+    v[2] = q.z;
+    v[3] = q.w;
+}
+__device__ __forceinline__ void lds_vec(const double* p, double (&v)[2]) {
+    const double2 q = *reinterpret_cast<const double2*>(p);
+    v[0] = q.x;
+    v[1] = q.y;
+}
+// GT values of a right-hand row (16-byte aligned when GT is a multiple of 16 bytes)
+template <class Cv, int GT>
+__device__ __forceinline__ void lds_rhs(const Cv* p, Cv (&v)[GT]) {
+    if constexpr (GT * sizeof(Cv) % 16 == 0) {
+#pragma unroll
+        for (int g = 0; g < GT; g += 16 / (int)sizeof(Cv)) {
+            Cv w[16 / sizeof(Cv)];
+            lds_vec(p + g, w);
+#pragma unroll
+            for (int k = 0; k < 16 / (int)sizeof(Cv); ++k) v[g + k] = w[k];
+        }
+    } else {
+#pragma unroll
+        for (int g = 0; g < GT; ++g) v[g] = p[g];
+    }
+}
+
+// Forward trailing rows [r0, r1) of an inverse front: f -= L[r0:r1, 0:w] y, by half tiles
+// of SB rows x SB/2 columns (tensor map `maps`: box {SB, SB/2}); the tiles start at r0
+// rounded down to 16 bytes.  Thread (row group, right-hand group, column split) keeps an
+// RT x GT tile of sums.
 template <class T, class Cv, int SB, int RG>
-__global__ void __launch_bounds__(256, 1) k_fwd_inv_tail(const SolveBlockTask* __restrict__ tasks, SolveArgs A,
+__global__ void __launch_bounds__(256, 2) k_fwd_inv_tail(const SolveBlockTask* __restrict__ tasks, SolveArgs A,
                                                          const CUtensorMap* __restrict__ maps,
                                                          const Cv* __restrict__ yv, Cv* __restrict__ fv, int* status) {
-    using R = LevelRhs<Cv, SB, RG>;
-    constexpr int TPR = R::TP, CPT = SB / TPR, RS = R::RS, FG = R::FG;
+    static_assert(sizeof(T) == sizeof(Cv), "factor and vector elements of one size");
+    using W = TailTiles<Cv, SB, RG>;
+    constexpr int HC = SB / 2, RT = W::RT, GT = W::GT, NG = W::NG, NH = W::NH, NS = W::NS, RS = W::RS;
+    constexpr int CPS = HC / NS;                          // columns of a half tile per split
     constexpr int kAlign = 16 / (int)sizeof(T);
+    constexpr unsigned kBytes = SB * HC * sizeof(T);
     extern __shared__ __align__(128) unsigned char blk_smem[];
     unsigned char* sm = blk_smem + ((1024u - (smem_addr(blk_smem) & 1023u)) & 1023u);
-    T* const stage0 = reinterpret_cast<T*>(sm);          // two tile stages
-    auto stage = [&](int k) { return stage0 + k * SB * SB; };
-    Cv* const yb0 = reinterpret_cast<Cv*>(stage0 + 2 * SB * SB);   // two blocks y_kb: SB rows x RG
-    auto ybuf = [&](int k) { return yb0 + k * SB * RS; };
-    Cv* part = yb0 + 2 * SB * RS;
+    T* const stage0 = reinterpret_cast<T*>(sm);          // two half-tile stages (SB x HC, column-major)
+    auto stage = [&](int k) { return stage0 + k * SB * HC; };
+    Cv* const yb0 = reinterpret_cast<Cv*>(stage0 + 2 * SB * HC);   // two blocks of y: HC rows x RG
+    auto ybuf = [&](int k) { return yb0 + k * HC * RS; };
+    Cv* const part = reinterpret_cast<Cv*>(stage0);      // after the last tile: NS x SB x RG
     __shared__ unsigned long long bar[2];
     const SolveBlockTask tk = tasks[blockIdx.x];
     const SnDev d = A.sn[tk.s];
-    const int nb = tk.kn, r0 = tk.r0, r1 = tk.r1, ra = r0 & ~(kAlign - 1);
-    const int tid = threadIdx.x, row = tid % SB, pid = tid / SB;
-    const bool fin = RG >= TPR || pid == 0;
-    const int g0 = RG >= TPR ? pid * FG : 0;
-    const int i = r0 + row, trow = min(row + (r0 - ra), SB - 1);
+    const int nh = (d.w + HC - 1) / HC, r0 = tk.r0, r1 = tk.r1, ra = r0 & ~(kAlign - 1);
+    const int tid = threadIdx.x, rgp = tid % NG, rh = (tid / NG) % NH, cs = tid / (NG * NH);
     const long long fo = A.fvec_off[tk.s];
     if (tid == 0) {
         bar_init(&bar[0]);
@@ -259,83 +334,97 @@ __global__ void __launch_bounds__(256, 1) k_fwd_inv_tail(const SolveBlockTask* _
     }
     __syncthreads();
     unsigned phase = 0;
-    RhsPrefetch<Cv, SB, RG> pf;
+    RhsPrefetch<Cv, HC, RG> pf;
     for (int rg = 0; rg < A.nrhs; rg += RG) {
         const int ng = min(RG, A.nrhs - rg);
-        auto fetch = [&](int kb) {
-            const int kn = min(SB, d.w - kb * SB);
+        auto fetch = [&](int h) {
+            const int kn = min(HC, d.w - h * HC);
             pf.fetch([&](int c, int g) {
-                return (g < ng && c < kn) ? yv[fo + (long long)(rg + g) * A.fv_stride + kb * SB + c] : Cv(0);
+                return (g < ng && c < kn) ? yv[fo + (long long)(rg + g) * A.fv_stride + h * HC + c] : Cv(0);
             });
         };
         fetch(0);
         if (tid == 0) {
-            start_bulk_tile<T, SB>(stage(0), maps + tk.s, ra, 0, &bar[0]);
-            if (nb > 1) start_bulk_tile<T, SB>(stage(1), maps + tk.s, ra, SB, &bar[1]);
+            start_box_tile(stage(0), maps + tk.s, ra, 0, kBytes, &bar[0]);
+            if (nh > 1) start_box_tile(stage(1), maps + tk.s, ra, HC, kBytes, &bar[1]);
         }
         pf.commit(ybuf(0));
-        if (nb > 1) fetch(1);
-        RhsAcc<Cv, RG> acc;
-        acc.zero();
-        for (int kb = 0; kb < nb; ++kb) {
-            if (!__syncthreads_and(bar_wait(&bar[kb & 1], (phase >> (kb & 1)) & 1u, status))) return;
-            phase ^= 1u << (kb & 1);
-            const T* tile = stage(kb & 1);
-            const Cv* yb = ybuf(kb & 1);
-#pragma unroll 2
-            for (int u0 = 0; u0 < CPT; u0 += 4)
+        if (nh > 1) fetch(1);
+        Cv acc[RT][GT];
 #pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const int c = pid * CPT + u0 + q;
-                    acc.add(q, (Cv)tile[trow + c * SB], yb + c * RS);
-                }
-            if (kb + 1 < nb) pf.commit(ybuf((kb + 1) & 1));
-            if (kb + 2 < nb) fetch(kb + 2);
-            __syncthreads();   // the stage is free again
-            if (tid == 0 && kb + 2 < nb) start_bulk_tile<T, SB>(stage(kb & 1), maps + tk.s, ra, (kb + 2) * SB, &bar[kb & 1]);
-        }
-        acc.store(part + (pid * SB + row) * RG);
-        __syncthreads();
-        if (fin && i < r1) {
+        for (int a = 0; a < RT; ++a)
 #pragma unroll
-            for (int q = 0; q < FG; ++q) {
-                const int g = g0 + q;
-                if (g >= ng) break;
-                Cv sum = part[row * RG + g];
+            for (int g = 0; g < GT; ++g) acc[a][g] = Cv(0);
+        for (int h = 0; h < nh; ++h) {
+            if (!__syncthreads_and(bar_wait(&bar[h & 1], (phase >> (h & 1)) & 1u, status))) return;
+            phase ^= 1u << (h & 1);
+            const T* tile = stage(h & 1) + rgp * RT;
+            const Cv* yb = ybuf(h & 1) + rh * GT;
+#pragma unroll 4
+            for (int u = 0; u < CPS; ++u) {
+                const int c = cs * CPS + u;
+                Cv l[RT], y[GT];
+                lds_vec(tile + c * SB, l);
+                lds_rhs<Cv, GT>(yb + c * RS, y);
 #pragma unroll
-                for (int p = 1; p < TPR; ++p) sum += part[(p * SB + row) * RG + g];
-                fv[fo + (long long)(rg + g) * A.fv_stride + i] -= sum;
+                for (int a = 0; a < RT; ++a)
+#pragma unroll
+                    for (int g = 0; g < GT; ++g) acc[a][g] += l[a] * y[g];
             }
+            if (h + 1 < nh) pf.commit(ybuf((h + 1) & 1));
+            if (h + 2 < nh) fetch(h + 2);
+            __syncthreads();   // the stage is free again
+            if (tid == 0 && h + 2 < nh) start_box_tile(stage(h & 1), maps + tk.s, ra, (h + 2) * HC, kBytes, &bar[h & 1]);
+        }
+        // partial sums of the column splits, then f -= their sum for the chunk's rows
+#pragma unroll
+        for (int a = 0; a < RT; ++a)
+#pragma unroll
+            for (int g = 0; g < GT; ++g) part[(cs * SB + rgp * RT + a) * RG + rh * GT + g] = acc[a][g];
+        __syncthreads();
+        for (int e = tid; e < SB * RG; e += blockDim.x) {
+            const int g = e / SB, lr = e - g * SB, i = ra + lr;
+            if (g >= ng || i < r0 || i >= r1) continue;
+            Cv sum = part[lr * RG + g];
+#pragma unroll
+            for (int p = 1; p < NS; ++p) sum += part[(p * SB + lr) * RG + g];
+            fv[fo + (long long)(rg + g) * A.fv_stride + i] -= sum;
         }
         __syncthreads();
     }
 }
 
-// Backward partial sums of column block kb of an inverse front against its trailing rows
-// [r0, r1): partial[(slot nrhs + r) SB + c] = sum_rows L[row, kb SB + c] g[row] (right-hand
-// side r).  Thread (column, part) sums its part of each tile's rows in skewed order.
+// Backward: column block kb of an inverse front against its trailing rows [r0, r1) (task
+// {s, kb, nb, r0, r1, nq, slot}), by half tiles of SB/2 rows x SB columns (tensor map `maps`:
+// box {SB/2, SB}), each transposed in shared memory so that a thread's RT columns are read
+// without bank conflicts and g is a broadcast.  Thread (column group, right-hand group, row
+// split) keeps an RT x GT tile of sums; column group q holds columns q + NG a.  The sums go
+// to partial slot `slot` ((slot nrhs + r) SB + c for right-hand side r, column c), which
+// k_bwd_inv_reduce adds to g of the block's columns.
 template <class T, class Cv, int SB, int RG>
-__global__ void __launch_bounds__(256, 1) k_bwd_inv_cols(const SolveBlockTask* __restrict__ tasks, SolveArgs A,
-                                                         const CUtensorMap* __restrict__ maps,
-                                                         const Cv* __restrict__ fv, Cv* __restrict__ partial,
-                                                         int* status) {
-    using R = LevelRhs<Cv, SB, RG>;
-    constexpr int TPC = R::TP, RPT = SB / TPC, RS = R::RS, FG = R::FG;
+__global__ void __launch_bounds__(256, 2) k_bwd_inv_cols(const SolveBlockTask* __restrict__ tasks, SolveArgs A,
+                                                         const CUtensorMap* __restrict__ maps, const Cv* __restrict__ fv,
+                                                         Cv* __restrict__ partial, int* status) {
+    static_assert(sizeof(T) == sizeof(Cv), "factor and vector elements of one size");
+    using W = TailTiles<Cv, SB, RG>;
+    constexpr int HR = SB / 2, RT = W::RT, GT = W::GT, NG = W::NG, NH = W::NH, NS = W::NS, RS = W::RS;
+    constexpr int RPS = HR / NS;                          // rows of a half tile per split
+    constexpr int TS = SB + 1;                            // row stride of the transposed half tile
     constexpr int kAlign = 16 / (int)sizeof(T);
+    constexpr unsigned kBytes = HR * SB * sizeof(T);
     extern __shared__ __align__(128) unsigned char blk_smem[];
     unsigned char* sm = blk_smem + ((1024u - (smem_addr(blk_smem) & 1023u)) & 1023u);
-    T* const stage0 = reinterpret_cast<T*>(sm);          // two tile stages
-    auto stage = [&](int k) { return stage0 + k * SB * SB; };
-    Cv* const xb0 = reinterpret_cast<Cv*>(stage0 + 2 * SB * SB);   // two blocks of g: SB rows x RG
-    auto xbuf = [&](int k) { return xb0 + k * SB * RS; };
-    Cv* part = xb0 + 2 * SB * RS;
+    T* const stage0 = reinterpret_cast<T*>(sm);          // two half-tile stages (HR x SB, column-major)
+    auto stage = [&](int k) { return stage0 + k * HR * SB; };
+    T* const tt = stage0 + 2 * HR * SB;                   // transposed half tile: row r at r TS
+    Cv* const xb0 = reinterpret_cast<Cv*>(tt + HR * TS);  // two blocks of g: HR rows x RG
+    auto xbuf = [&](int k) { return xb0 + k * HR * RS; };
+    Cv* const part = reinterpret_cast<Cv*>(stage0);      // after the last tile: NS x SB x RG
     __shared__ unsigned long long bar[2];
     const SolveBlockTask tk = tasks[blockIdx.x];
     const int kb = tk.k0, r0 = tk.r0, r1 = tk.r1, ra = r0 & ~(kAlign - 1);
-    const int ntile = (r1 - ra + SB - 1) / SB;
-    const int tid = threadIdx.x, ccol = tid % SB, cpart = tid / SB;
-    const bool fin = RG >= TPC || cpart == 0;
-    const int g0 = RG >= TPC ? cpart * FG : 0;
+    const int ntile = (r1 - ra + HR - 1) / HR;
+    const int tid = threadIdx.x, cgp = tid % NG, rh = (tid / NG) % NH, rsp = tid / (NG * NH);
     const long long fo = A.fvec_off[tk.s];
     if (tid == 0) {
         bar_init(&bar[0]);
@@ -343,11 +432,11 @@ __global__ void __launch_bounds__(256, 1) k_bwd_inv_cols(const SolveBlockTask* _
     }
     __syncthreads();
     unsigned phase = 0;
-    RhsPrefetch<Cv, SB, RG> pf;
+    RhsPrefetch<Cv, HR, RG> pf;
     for (int rg = 0; rg < A.nrhs; rg += RG) {
         const int ng = min(RG, A.nrhs - rg);
         auto fetch = [&](int t) {
-            const int tr = ra + t * SB;
+            const int tr = ra + t * HR;
             pf.fetch([&](int r, int g) {
                 const int gr = tr + r;
                 return (g < ng && gr >= r0 && gr < r1) ? fv[fo + (long long)(rg + g) * A.fv_stride + gr] : Cv(0);
@@ -355,55 +444,100 @@ __global__ void __launch_bounds__(256, 1) k_bwd_inv_cols(const SolveBlockTask* _
         };
         fetch(0);
         if (tid == 0) {
-            start_bulk_tile<T, SB>(stage(0), maps + tk.s, ra, kb * SB, &bar[0]);
-            if (ntile > 1) start_bulk_tile<T, SB>(stage(1), maps + tk.s, ra + SB, kb * SB, &bar[1]);
+            start_box_tile(stage(0), maps + tk.s, ra, kb * SB, kBytes, &bar[0]);
+            if (ntile > 1) start_box_tile(stage(1), maps + tk.s, ra + HR, kb * SB, kBytes, &bar[1]);
         }
         pf.commit(xbuf(0));
         if (ntile > 1) fetch(1);
-        RhsAcc<Cv, RG> acc;
-        acc.zero();
+        Cv acc[RT][GT];
+#pragma unroll
+        for (int a = 0; a < RT; ++a)
+#pragma unroll
+            for (int g = 0; g < GT; ++g) acc[a][g] = Cv(0);
         for (int t = 0; t < ntile; ++t) {
             if (!__syncthreads_and(bar_wait(&bar[t & 1], (phase >> (t & 1)) & 1u, status))) return;
             phase ^= 1u << (t & 1);
-            const T* tile = stage(t & 1);
-            const Cv* xb = xbuf(t & 1);
-#pragma unroll 2
-            for (int u0 = 0; u0 < RPT; u0 += 4)
+            {
+                // 16 bytes (RT consecutive rows of one column) per read
+                const T* src = stage(t & 1);
+                constexpr int QR = HR / RT;   // 16-byte groups per column
+                for (int e = tid; e < QR * SB; e += blockDim.x) {
+                    const int r = (e % QR) * RT, c = e / QR;
+                    T v[RT];
+                    lds_vec(src + c * HR + r, v);
 #pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const int r = cpart * RPT + ((u0 + q + ccol) & (RPT - 1));
-                    acc.add(q, (Cv)tile[r + ccol * SB], xb + r * RS);
+                    for (int k = 0; k < RT; ++k) tt[(r + k) * TS + c] = v[k];
                 }
+            }
+            __syncthreads();   // tt is ready, the stage is free again
+            if (tid == 0 && t + 2 < ntile) start_box_tile(stage(t & 1), maps + tk.s, ra + (t + 2) * HR, kb * SB, kBytes, &bar[t & 1]);
+            const Cv* xb = xbuf(t & 1) + rh * GT;
+#pragma unroll 4
+            for (int u = 0; u < RPS; ++u) {
+                const int r = rsp * RPS + u;
+                Cv l[RT], x[GT];
+#pragma unroll
+                for (int a = 0; a < RT; ++a) l[a] = (Cv)tt[r * TS + cgp + NG * a];
+                lds_rhs<Cv, GT>(xb + r * RS, x);
+#pragma unroll
+                for (int a = 0; a < RT; ++a)
+#pragma unroll
+                    for (int g = 0; g < GT; ++g) acc[a][g] += l[a] * x[g];
+            }
             if (t + 1 < ntile) pf.commit(xbuf((t + 1) & 1));
             if (t + 2 < ntile) fetch(t + 2);
-            __syncthreads();
-            if (tid == 0 && t + 2 < ntile) start_bulk_tile<T, SB>(stage(t & 1), maps + tk.s, ra + (t + 2) * SB, kb * SB, &bar[t & 1]);
+            __syncthreads();   // tt and the right-hand block are free again
         }
-        acc.store(part + (cpart * SB + ccol) * RG);
+#pragma unroll
+        for (int a = 0; a < RT; ++a)
+#pragma unroll
+            for (int g = 0; g < GT; ++g) part[(rsp * SB + cgp + NG * a) * RG + rh * GT + g] = acc[a][g];
         __syncthreads();
-        if (fin) {
+        for (int e = tid; e < SB * RG; e += blockDim.x) {
+            const int g = e / SB, c = e - g * SB;
+            if (g >= ng) continue;
+            Cv sum = part[c * RG + g];
 #pragma unroll
-            for (int q = 0; q < FG; ++q) {
-                const int g = g0 + q;
-                if (g >= ng) break;
-                Cv sum = part[ccol * RG + g];
-#pragma unroll
-                for (int p = 1; p < TPC; ++p) sum += part[(p * SB + ccol) * RG + g];
-                partial[((long long)tk.blk * A.nrhs + rg + g) * SB + ccol] = sum;
-            }
+            for (int p = 1; p < NS; ++p) sum += part[(p * SB + c) * RG + g];
+            partial[((long long)tk.blk * A.nrhs + rg + g) * SB + c] = sum;
         }
         __syncthreads();
     }
 }
 
-// Backward x_j = sum_{i >= j} Linv(i, j)^T g_i, g_i = the gathered block minus its nq partial
-// sums (slots slot0 + i nq + q, added in order), right-hand sides [RG blockIdx.y, +RG);
-// writes x_j to the work vector.
+// Backward: g of column block kb of an inverse front -= its nq partial sums, added in chunk
+// order (task {s, kb, nb, slot0, nq, -, -}: the block's chunks have slots slot0 .. slot0+nq-1),
+// one CTA per block and right-hand side (blockIdx.y), one thread per column.
+template <class Cv, int SB>
+__global__ void __launch_bounds__(SB) k_bwd_inv_reduce(const SolveBlockTask* __restrict__ tasks, SolveArgs A,
+                                                       Cv* __restrict__ fv, const Cv* __restrict__ partial) {
+    const SolveBlockTask tk = tasks[blockIdx.x];
+    const SnDev d = A.sn[tk.s];
+    const int kb = tk.k0, slot0 = tk.r0, nq = tk.r1, c = threadIdx.x;
+    if (kb * SB + c >= d.w) return;
+    for (int r = blockIdx.y; r < A.nrhs; r += gridDim.y) {
+        Cv* gp = fv + A.fvec_off[tk.s] + (long long)r * A.fv_stride + kb * SB + c;
+        Cv v = *gp;
+        const Cv* pp = partial + ((long long)slot0 * A.nrhs + r) * SB + c;
+        for (int q0 = 0; q0 < nq; q0 += 8) {   // eight loads in flight, subtracted in chunk order
+            Cv p8[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) p8[k] = q0 + k < nq ? pp[(long long)(q0 + k) * A.nrhs * SB] : Cv(0);
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+                if (q0 + k < nq) v -= p8[k];
+        }
+        *gp = v;
+    }
+}
+
+// Backward x_j = sum_{i >= j} Linv(i, j)^T g_i (g_i already reduced by k_bwd_inv_cols),
+// right-hand sides [RG blockIdx.y, +RG); writes x_j to the work vector.
 template <class T, class Cv, int SB, int RG>
 __global__ void __launch_bounds__(256, 1) k_bwd_inv_diag(const SolveBlockTask* __restrict__ tasks, SolveArgs A,
                                                          const Cv* __restrict__ linv, const Cv* __restrict__ linv_off,
-                                                         const Cv* __restrict__ fv, const Cv* __restrict__ partial,
-                                                         Cv* __restrict__ work, int* status) {
+                                                         const Cv* __restrict__ fv, Cv* __restrict__ work,
+                                                         int* status) {
     using R = LevelRhs<Cv, SB, RG>;
     constexpr int TPC = R::TP, RPT = SB / TPC, RS = R::RS, FG = R::FG;
     extern __shared__ __align__(128) unsigned char blk_smem[];
@@ -416,7 +550,7 @@ __global__ void __launch_bounds__(256, 1) k_bwd_inv_diag(const SolveBlockTask* _
     __shared__ unsigned long long bar[2];
     const SolveBlockTask tk = tasks[blockIdx.x];
     const SnDev d = A.sn[tk.s];
-    const int j = tk.k0, nb = tk.kn, ob = tk.r0, slot0 = tk.r1, nq = tk.flags, blk = tk.blk;
+    const int j = tk.k0, nb = tk.kn, ob = tk.r0, blk = tk.blk;
     const int rg = blockIdx.y * RG, ng = min(RG, A.nrhs - rg);
     const int tid = threadIdx.x, ccol = tid % SB, cpart = tid / SB;
     const bool fin = RG >= TPC || cpart == 0;
@@ -439,13 +573,7 @@ __global__ void __launch_bounds__(256, 1) k_bwd_inv_diag(const SolveBlockTask* _
     auto fetch = [&](int i) {
         pf.fetch([&](int c, int g) {
             const int col = i * SB + c;
-            Cv v = Cv(0);
-            if (g < ng && col < d.w) {
-                v = fv[fo + (long long)(rg + g) * A.fv_stride + col];
-                const Cv* pp = partial + ((long long)(slot0 + i * nq) * A.nrhs + rg + g) * SB + c;
-                for (int q = 0; q < nq; ++q) v -= pp[(long long)q * A.nrhs * SB];
-            }
-            return v;
+            return (g < ng && col < d.w) ? fv[fo + (long long)(rg + g) * A.fv_stride + col] : Cv(0);
         });
     };
     fetch(j);

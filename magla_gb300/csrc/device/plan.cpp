@@ -620,10 +620,10 @@ Plan build_from_fronts(int n, int count, const int* first_column, const int* par
         if (solo.count > 0) P.bwd_launches.push_back(solo);
         if (!multi.empty()) P.bwd_launches.push_back(level_launch(SolveLaunch::BwdLevel, multi, false));
         if (!inv.empty()) {
-            // partial sums per (column block, chunk of kInvColRowsPlan trailing rows), then x_1 per
-            // block column, which adds its blocks' partial sums in chunk order
+            // partial sums per (column block, chunk of kInvColRowsPlan trailing rows), their sums
+            // per column block in chunk order, then x_1 per block column
             int b = (int)P.solve_tasks.size(), slots = 0;
-            std::vector<SolveBlockTask> diag_tasks;
+            std::vector<SolveBlockTask> diag_tasks, reduce_tasks;
             for (int s : inv) {
                 const SnDev& d = P.sn[s];
                 const int nb = (d.w + SB - 1) / SB;
@@ -633,10 +633,17 @@ Plan build_from_fronts(int n, int count, const int* first_column, const int* par
                         const int r0 = d.w + q * kInvColRowsPlan;
                         P.solve_tasks.push_back({s, kb, nb, r0, std::min(d.m, r0 + kInvColRowsPlan), 0, slots + kb * nq + q});
                     }
-                for (int j = 0; j < nb; ++j) diag_tasks.push_back({s, j, nb, inv_ob[s], slots, nq, first_blk[s]});
+                if (nq > 0)
+                    for (int kb = 0; kb < nb; ++kb) reduce_tasks.push_back({s, kb, nb, slots + kb * nq, nq, 0, 0});
+                for (int j = 0; j < nb; ++j) diag_tasks.push_back({s, j, nb, inv_ob[s], 0, 0, first_blk[s]});
                 slots += nb * nq;
             }
             if ((int)P.solve_tasks.size() > b) P.bwd_launches.push_back(simple(SolveLaunch::BwdInvCols, b));
+            if (!reduce_tasks.empty()) {
+                b = (int)P.solve_tasks.size();
+                P.solve_tasks.insert(P.solve_tasks.end(), reduce_tasks.begin(), reduce_tasks.end());
+                P.bwd_launches.push_back(simple(SolveLaunch::BwdInvReduce, b));
+            }
             P.inv_partial_slots = std::max(P.inv_partial_slots, slots);
             b = (int)P.solve_tasks.size();
             P.solve_tasks.insert(P.solve_tasks.end(), diag_tasks.begin(), diag_tasks.end());

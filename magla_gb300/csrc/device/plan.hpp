@@ -64,7 +64,7 @@ struct Launch {
 struct SolveLaunch {
     enum Kind : int {
         FwdGather, FwdSolo, FwdLevel, BwdGather, BwdTail, BwdSolo, BwdLevel, FwdTail, BwdTailReduce,
-        FwdInvDiag, FwdInvTail, BwdInvCols, BwdInvDiag, KindCount
+        FwdInvDiag, FwdInvTail, BwdInvCols, BwdInvDiag, BwdInvReduce, KindCount
     } kind;
     int begin, count;   // tasks; level launches: the chains (one per front)
     int steps;          // level launches: most diagonal blocks of one front of the level
@@ -84,9 +84,9 @@ struct SolveLaunch {
 //   FwdInvDiag           {s, i, nb, ob_s, -, -, blk}: y_i = sum_{j <= i} Linv(i, j) f_j;
 //   FwdInvTail           {s, -, nb, r0, r1, -, -}: f[r0, r1) -= L[r0:r1, 0:w] y;
 //   BwdInvCols           {s, kb, nb, r0, r1, -, slot}: partial sums of L[r0:r1, block kb]^T g
-//                        into partial slot `slot`;
-//   BwdInvDiag           {s, j, nb, ob_s, slot0, nq, blk}: g_i -= its nq partial slots
-//                        slot0 + i nq + (0 .. nq-1), then x_j = sum_{i >= j} Linv(i, j)^T g_i.
+//                        into partial slot `slot` (a block's nq chunks have consecutive slots);
+//   BwdInvReduce         {s, kb, nb, slot0, nq, -, -}: g of block kb -= its nq partial sums;
+//   BwdInvDiag           {s, j, nb, ob_s, -, -, blk}: x_j = sum_{i >= j} Linv(i, j)^T g_i.
 // blk is the diagonal-inverse index of the front's block 0.
 struct InvLaunch {
     int begin, count;   // inversion tasks of one diagonal i - j

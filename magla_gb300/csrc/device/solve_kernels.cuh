@@ -200,16 +200,22 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned by
                  : "memory");
 }
 // Waits (bounded) for phase `parity` of the mbarrier; false if the wait expired.
+// The clock is read only once the first try has failed (copies issued a tile ahead have
+// usually landed by then).
+__device__ __forceinline__ bool bar_try(unsigned long long* bar, unsigned parity) {
+    unsigned done;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return done != 0;
+}
 __device__ __forceinline__ bool bar_wait(unsigned long long* bar, unsigned parity, int* status) {
+    if (bar_try(bar, parity)) return true;
     const unsigned long long t0 = solve_ns();
     for (;;) {
-        unsigned done;
-        asm volatile(
-            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
-            : "=r"(done)
-            : "r"(smem_addr(bar)), "r"(parity)
-            : "memory");
-        if (done) return true;
+        if (bar_try(bar, parity)) return true;
         if (solve_ns() - t0 > kSolveWaitNs) {
             atomicExch(status, kSolveStatusTimeout);
             return false;
