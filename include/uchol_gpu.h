@@ -241,6 +241,30 @@ int uchol_residual_norms_static(int n, int nnz, int nrhs, const int* d_row_ptr, 
                                 double* d_norms, void* stream);
 const char* uchol_residual_norms_static_error(void);
 
+/* Kernel checks: one launch of a factorisation kernel of the mixed path on caller data
+ * (host buffers), so that tests can compare each kernel with an FP64 computation on the
+ * same operands.  No counterpart in the reference, whose numeric phase is one CPU routine.
+ *
+ * uchol_check_schur_update: the tensor-core Schur update (k_tc_gemm) of one job,
+ * C[rows, cols] -= W[rows, kbeg:kbeg+kn] L[cols, kbeg:kbeg+kn]^T over the lower triangle of
+ * result columns [c0, cend) (all in the panel, c < w, or all in the contribution block) of
+ * a front of m rows and w columns.  front / front_out: column-major m x m (lower triangle);
+ * w_op, l_op: row-major m x ld FP32 operands (ld a multiple of 64; BF16 rounds them to
+ * nearest even first); K runs in whole 128-byte blocks, so the operand columns from kbeg + kn
+ * to the end of its block must be zero (as the factorisation's staging copies are).  max_ctas > 0 caps the grid, which decides whether the launch is split
+ * in K (stream-K).  Outputs the tile count and whether the launch was split. */
+int uchol_check_schur_update(int bf16, int m, int w, int c0, int cend, int kbeg, int kn, const float* front,
+                             const float* w_op, const float* l_op, int ld, int max_ctas, float* front_out,
+                             int64_t* tiles_out, int* split_out);
+/* uchol_check_diag_panel: the outer block of the mixed path (k_diag_block + k_panel_solve) on
+ * the first nb <= 128 columns of an m-row front: front, l_out column-major m x nb (l_out: unit
+ * L11 and L21), d_out the nb FP64 pivots, w_stage_out (optional) the staged W = L D rows,
+ * column-major m x nb (rows >= nb); counts_out = {regularized, negative, failed column or -1}
+ * under the pivot rule !(d > threshold) with the given regularization value. */
+int uchol_check_diag_panel(int m, int nb, const float* front, double threshold, double regularization,
+                           int allow_regularization, float* l_out, double* d_out, float* w_stage_out,
+                           int* counts_out);
+
 /* Number of kernel launches this library has issued since it was loaded. */
 int64_t uchol_kernel_launches(void);
 /* Per-phase device timing of factorisations (one CUDA event pair per launch);

@@ -153,6 +153,11 @@ GPU_SYMBOLS = {
     "uchol_residual_norms_static_error": (C.c_char_p, []),
     "uchol_autotune": (C.c_int, [C.c_void_p, C.c_int, C.c_int, c_double_p, C.POINTER(Options), C.POINTER(Options),
                                  C.POINTER(AutotuneReport)]),
+    "uchol_check_schur_update": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                           C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p,
+                                           C.POINTER(C.c_int64), c_int_p]),
+    "uchol_check_diag_panel": (C.c_int, [C.c_int, C.c_int, C.c_void_p, C.c_double, C.c_double, C.c_int, C.c_void_p,
+                                         C.c_void_p, C.c_void_p, c_int_p]),
     "uchol_kernel_launches": (C.c_int64, []),
     "uchol_set_phase_timing": (None, [C.c_int]),
     "uchol_last_error": (C.c_char_p, []),

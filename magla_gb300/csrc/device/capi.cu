@@ -1540,3 +1540,5 @@ int uchol_residual_norms(uchol_factor f, int n, int nrhs, const double* b, int l
 }
 
 }  // extern "C"
+
+#include "kernel_checks.cuh"

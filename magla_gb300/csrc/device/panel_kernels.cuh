@@ -16,9 +16,13 @@
 // Together they replace the reference's per-column panel loop for these
 // blocks (CAESolvers/UCHOL/UtduNumericFactorization.cs:520-610): the same
 // L, D and pivot rule, computed in two launches per 128 columns instead of a
-// chain of small steps.  The fronts of the mixed path are stored in FP32, and
-// this GPU's FP32 rate is ~60x its FP64 rate, so no FP64 arithmetic appears
-// in either kernel; the FP64 residual refinement recovers full accuracy.
+// chain of small steps.  The fronts of the mixed path are stored in FP32 and L,
+// X and the products are FP32; the pivots are FP64: each diagonal entry of the
+// block is carried in FP64 through every elimination step inside the block
+// (d_r -= d_k L_rk^2 with the FP32 L), and the pivot test !(d > tol * scale),
+// the regularisation and D itself are FP64 (the FP32 elimination divides by D
+// rounded to FP32).  That is O(nb^2) FP64 work per block.  The FP64 residual
+// refinement recovers full accuracy of the solution.
 #pragma once
 
 #include <cfloat>
@@ -35,24 +39,27 @@ constexpr int kDiagLd = kDiagMax + 1;
 // and beyond nb), then D and D^{-1} (kDiagMax floats each)
 constexpr int kMinvStride = kDiagMax * kDiagMax + 2 * kDiagMax;
 constexpr int kSolveRows = 128;
-constexpr size_t kDiagSmemBytes = sizeof(float) * (2 * kDiagMax * kDiagLd + kDiagMax * 33 + 2 * kDiagMax);
+// float part: S and X (kDiagMax x kDiagLd each), Wt (kDiagMax x 33), D and D^{-1} in FP32;
+// then the FP64 part: the running diagonal and D (kDiagMax doubles each)
+constexpr size_t kDiagSmemFloats = 2 * kDiagMax * kDiagLd + kDiagMax * 33 + 2 * kDiagMax;
+constexpr size_t kDiagSmemBytes = sizeof(float) * kDiagSmemFloats + sizeof(double) * 2 * kDiagMax;
+static_assert(sizeof(float) * kDiagSmemFloats % sizeof(double) == 0, "the FP64 part is aligned");
 
 // Pivot acceptance of the reference, !(d > tol*scale) -> regularise or reject,
-// on FP32 pivots.  thr is the FP64 threshold rounded down to FP32, for which
-// (float)x > thr <=> (double)x > threshold holds for every float x.
-struct PivotAccF {
+// on FP64 pivots (UtduNumericFactorization.cs:553-592).
+struct PivotAccD {
     int regularized = 0, negative = 0, failed = INT_MAX, accepted = 0;
-    float lo = FLT_MAX, hi = 0.f;
-    __device__ __forceinline__ float accept(float piv, int column, float thr, float reg, int allow) {
+    double lo = DBL_MAX, hi = 0.0;
+    __device__ __forceinline__ double accept(double piv, int column, double thr, double reg, int allow) {
         if (!(piv > thr)) {
             if (!allow) failed = min(failed, column);
-            if (piv < 0.f) ++negative;
+            if (piv < 0.0) ++negative;
             ++regularized;
             piv = reg;
         }
-        const float a = fabsf(piv);
-        lo = fminf(lo, a);
-        hi = fmaxf(hi, a);
+        const double a = fabs(piv);
+        lo = fmin(lo, a);
+        hi = fmax(hi, a);
         ++accepted;
         return piv;
     }
@@ -61,8 +68,8 @@ struct PivotAccF {
         if (negative) atomicAdd(&st->negative, negative);
         if (failed != INT_MAX) atomicMin(&st->failed, failed);
         if (accepted) {
-            atomicMin(&st->min_bits, (unsigned long long)__double_as_longlong((double)lo));
-            atomicMax(&st->max_bits, (unsigned long long)__double_as_longlong((double)hi));
+            atomicMin(&st->min_bits, (unsigned long long)__double_as_longlong(lo));
+            atomicMax(&st->max_bits, (unsigned long long)__double_as_longlong(hi));
         }
     }
 };
@@ -76,7 +83,9 @@ __device__ __forceinline__ float rcp_approx(float x) {
 // LDL^T of the bn x bn (bn <= 32) diagonal sub-block at S[b0][b0] by one
 // warp, with the same eliminations applied to the identity so that
 // X_bb = L_bb^{-1} comes out with it.  Lane r holds row b0 + r in registers
-// as a shift register: at pivot k, a[j] is F[r][k + j] and x[c] is X[r][c].
+// as a shift register: at pivot k, a[j] is F[r][k + j] and x[c] is X[r][c];
+// its diagonal entry is carried separately in FP64 (dd, from dg), and the pivot
+// d_k is lane k's dd.
 // Every lane below the pivot applies F[r][k+j] -= L[r][k] (d_k L[k+j][k])
 // (the reference's association) and shifts its row by one, so the loop over
 // pivots stays rolled (short code) while every register index is a constant.
@@ -85,26 +94,32 @@ __device__ __forceinline__ float rcp_approx(float x) {
 // loads each: lane r stores d_k L[r][k] at slot (r - k) mod 32, so slot j is
 // row k + j (rows above the pivot store zero).  Entries right of the
 // diagonal take meaningless updates and are never read.
-__device__ __forceinline__ void warp_ldlt32(float* S, float* X, int b0, int bn, int lane, int col0, float thr,
-                                            float reg, int allow, float* sd, float* sdi, PivotAccF& acc,
-                                            float* scr) {
+__device__ __forceinline__ void warp_ldlt32(float* S, float* X, int b0, int bn, int lane, int col0, double thr,
+                                            double reg, int allow, float* sd, float* sdi, double* dg, double* sd64,
+                                            PivotAccD& acc, float* scr) {
     float a[32], x[32];
 #pragma unroll
     for (int j = 0; j < 32; ++j) {
         a[j] = (lane < bn && j <= lane) ? S[(b0 + lane) * kDiagLd + b0 + j] : 0.f;
         x[j] = j == lane ? 1.f : 0.f;
     }
+    double dd = lane < bn ? dg[b0 + lane] : 0.0;   // this row's diagonal entry, FP64
     for (int k = 0; k < bn; ++k) {
-        const float raw = __shfl_sync(0xffffffffu, a[0], k);   // F[k][k]
-        const float piv = acc.accept(raw, col0 + k, thr, reg, allow);   // the same in every lane
+        const double raw = __shfl_sync(0xffffffffu, dd, k);   // F[k][k]
+        const double piv64 = acc.accept(raw, col0 + k, thr, reg, allow);   // the same in every lane
+        const float piv = (float)piv64;
         const float inv = rcp_approx(piv);
         const bool below = lane > k && lane < bn;
         const float l = below ? a[0] * inv : 0.f;
-        if (below) S[(b0 + lane) * kDiagLd + b0 + k] = l;
+        if (below) {
+            S[(b0 + lane) * kDiagLd + b0 + k] = l;
+            dd -= piv64 * ((double)l * (double)l);
+        }
         if (lane == k) {
             S[(b0 + k) * kDiagLd + b0 + k] = 1.f;
             sd[b0 + k] = piv;
             sdi[b0 + k] = inv;
+            sd64[b0 + k] = piv64;
         }
         scr[(lane - k) & 31] = piv * l;
         if (lane == k) {
@@ -151,11 +166,12 @@ __global__ void __launch_bounds__(256, 1) k_diag_block(const PanelTask* __restri
     float* Wt = X + kDiagMax * kDiagLd;      // W = L D of the current sub-block's rows below it
     float* sd = Wt + kDiagMax * 33;          // D
     float* sdi = sd + kDiagMax;              // D^{-1}
+    double* dg = reinterpret_cast<double*>(smem + kDiagSmemFloats);   // running diagonal, FP64
+    double* sd64 = dg + kDiagMax;            // D, FP64
     const PanelTask tk = tasks[blockIdx.x];
     const SnDev d = sn[tk.s];
     const FactorCtl ctl = *ctlp;
-    const float thr = __double2float_rd(ctl.threshold);
-    const float reg = (float)ctl.regularization;
+    const double thr = ctl.threshold, reg = ctl.regularization;
     const int nb = tk.nb, k0 = tk.j0;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     float* P = panel + d.panel_off + k0 + (long long)k0 * d.ldp;   // A11 origin, column-major, ld = ldp
@@ -175,15 +191,16 @@ __global__ void __launch_bounds__(256, 1) k_diag_block(const PanelTask* __restri
             S[r * kDiagLd + c] = v[q];
         }
     }
+    if (tid < kDiagMax) dg[tid] = tid < nb ? (double)P[tid + (long long)tid * d.ldp] : 0.0;
     __syncthreads();
 
-    PivotAccF acc;
+    PivotAccD acc;
     for (int b0 = 0; b0 < nb; b0 += 32) {
         const int bn = min(32, nb - b0);
         // (1) LDL^T of the sub-block and X_bb = L_bb^{-1}, by one warp
         if (warp == 0)   // Wt is free until step (3): its first 64 floats are the warp's scratch
-            warp_ldlt32(S, X, b0, bn, lane, d.first_col + k0 + b0, thr, reg, ctl.allow_regularization, sd, sdi, acc,
-                        Wt);
+            warp_ldlt32(S, X, b0, bn, lane, d.first_col + k0 + b0, thr, reg, ctl.allow_regularization, sd, sdi, dg,
+                        sd64, acc, Wt);
         __syncthreads();
         // (3) rows below the sub-block: w[r][j] = sum_{k<=j} A[r][b0+k] X_bb[j][k], l = w / d_j;
         //     lane j, rows r0 + 8 q (four independent sums per lane)
@@ -214,6 +231,25 @@ __global__ void __launch_bounds__(256, 1) k_diag_block(const PanelTask* __restri
             }
         }
         __syncthreads();
+        // (3b) the diagonal entries of the rows below, in FP64: d_r -= sum_k d_k L_rk^2, two threads per
+        //      row (16 of the sub-block's columns each, four independent sums); reads only the
+        //      sub-block's columns of S, which step (4) does not write
+        {
+            const int r = rb0 + (tid >> 1), kh = (tid & 1) * 16;
+            double v[4] = {0.0, 0.0, 0.0, 0.0};
+            if (r < nb) {
+#pragma unroll
+                for (int k = 0; k < 16; ++k) {
+                    if (kh + k < bn) {
+                        const double l = (double)S[r * kDiagLd + b0 + kh + k];
+                        v[k & 3] += sd64[b0 + kh + k] * (l * l);
+                    }
+                }
+            }
+            double sum = (v[0] + v[1]) + (v[2] + v[3]);
+            sum += __shfl_xor_sync(0xffffffffu, sum, 1);
+            if (r < nb && kh == 0) dg[r] -= sum;
+        }
         // (4) trailing update of the block: S[r][c] -= sum_k W[r][k] L[c][k], rb0 <= c <= r < nb
         if (rb0 < nb) {
             const int tx = tid & 15, ty = tid >> 4;
@@ -316,7 +352,7 @@ __global__ void __launch_bounds__(256, 1) k_diag_block(const PanelTask* __restri
     // (6) write L11 (unit diagonal), D, and the workspace slot
     for (int c = warp; c < nb; c += 8)
         for (int r = c + lane; r < nb; r += 32) P[r + (long long)c * d.ldp] = r == c ? 1.f : S[r * kDiagLd + c];
-    if (tid < nb) diag[d.first_col + k0 + tid] = (double)sd[tid];
+    if (tid < nb) diag[d.first_col + k0 + tid] = sd64[tid];
     float* M = minv + (size_t)tk.slot * kMinvStride;
     for (int idx = tid; idx < kDiagMax * kDiagMax; idx += 256) {
         const int k = idx >> 7, j = idx & (kDiagMax - 1);

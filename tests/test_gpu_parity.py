@@ -219,6 +219,21 @@ def test_indefinite_matrix_reports_negative_pivot(gpu_lib):
     assert f.NegativePivotCount == of.NegativePivotCount
 
 
+@pytest.mark.parametrize("precision", [Precision.TF32, Precision.BF16])
+@pytest.mark.parametrize("fixture", [F.singular, F.indefinite])
+def test_mixed_pivot_counts_match_the_fp64_path(gpu_lib, precision, fixture):
+    """The mixed path's pivot blocks apply the reference's rule in FP64: the same regularised and
+    negative counts as the FP64 oracle.  Bucket mask 0x10 sends these small fronts to the blocked
+    kernels (k_diag_block) instead of the whole-front FP64 kernel."""
+    m = fixture()
+    f = solver(Precision=precision, SmallFrontBuckets=0x10).Factorize(m)
+    sym, of = oracle_for(m)
+    assert f.RegularizedPivotCount == of.RegularizedPivotCount
+    assert f.NegativePivotCount == of.NegativePivotCount
+    with pytest.raises(InvalidOperationException):
+        solver(Precision=precision, SmallFrontBuckets=0x10, AllowDiagonalRegularization=False).Factorize(m)
+
+
 def test_run_twice_is_bitwise_deterministic(gpu_lib):
     m = G.grid_matrix(9, 9, 9, 2)
     b = build_vector(m.Size, 17)
@@ -258,7 +273,8 @@ def test_mixed_precision_refined_reaches_tolerance(gpu_lib, precision, builder):
     assert f.LastRefinement.initial_relative_residual < 3e-2
     assert f.LastRefinement.iterations <= 12
     assert max_relative_difference(x, x64) < 1e-6
-    # pivots of the FP64 pivot blocks stay close to the FP64 factor's
+    # the pivots (FP64 inside each pivot block, after low-precision Schur updates) stay close
+    # to the FP64 factor's
     assert max_relative_difference(f.Diagonal, f64.Diagonal) < 0.05
 
 
