@@ -46,10 +46,11 @@ constexpr size_t kDiagSmemBytes = sizeof(float) * kDiagSmemFloats + sizeof(doubl
 static_assert(sizeof(float) * kDiagSmemFloats % sizeof(double) == 0, "the FP64 part is aligned");
 
 // Pivot acceptance of the reference, !(d > tol*scale) -> regularise or reject,
-// on FP64 pivots (UtduNumericFactorization.cs:553-592).
+// on FP64 pivots (UtduNumericFactorization.cs:553-592).  Only the decision is
+// taken per pivot; the smallest and largest |d| of the block are taken from D
+// once it is complete (FP64 instructions are scarce on this GPU).
 struct PivotAccD {
-    int regularized = 0, negative = 0, failed = INT_MAX, accepted = 0;
-    double lo = DBL_MAX, hi = 0.0;
+    int regularized = 0, negative = 0, failed = INT_MAX;
     __device__ __forceinline__ double accept(double piv, int column, double thr, double reg, int allow) {
         if (!(piv > thr)) {
             if (!allow) failed = min(failed, column);
@@ -57,20 +58,12 @@ struct PivotAccD {
             ++regularized;
             piv = reg;
         }
-        const double a = fabs(piv);
-        lo = fmin(lo, a);
-        hi = fmax(hi, a);
-        ++accepted;
         return piv;
     }
     __device__ __forceinline__ void flush(PivotStats* st) const {
         if (regularized) atomicAdd(&st->regularized, regularized);
         if (negative) atomicAdd(&st->negative, negative);
         if (failed != INT_MAX) atomicMin(&st->failed, failed);
-        if (accepted) {
-            atomicMin(&st->min_bits, (unsigned long long)__double_as_longlong(lo));
-            atomicMax(&st->max_bits, (unsigned long long)__double_as_longlong(hi));
-        }
     }
 };
 
@@ -113,7 +106,8 @@ __device__ __forceinline__ void warp_ldlt32(float* S, float* X, int b0, int bn, 
         const float l = below ? a[0] * inv : 0.f;
         if (below) {
             S[(b0 + lane) * kDiagLd + b0 + k] = l;
-            dd -= piv64 * ((double)l * (double)l);
+            const double ld = (double)l;
+            dd = fma(-piv64, ld * ld, dd);   // l^2 is exact in FP64
         }
         if (lane == k) {
             S[(b0 + k) * kDiagLd + b0 + k] = 1.f;
@@ -242,7 +236,7 @@ __global__ void __launch_bounds__(256, 1) k_diag_block(const PanelTask* __restri
                 for (int k = 0; k < 16; ++k) {
                     if (kh + k < bn) {
                         const double l = (double)S[r * kDiagLd + b0 + kh + k];
-                        v[k & 3] += sd64[b0 + kh + k] * (l * l);
+                        v[k & 3] = fma(sd64[b0 + kh + k], l * l, v[k & 3]);
                     }
                 }
             }
@@ -363,6 +357,23 @@ __global__ void __launch_bounds__(256, 1) k_diag_block(const PanelTask* __restri
         M[kDiagMax * kDiagMax + kDiagMax + tid] = tid < nb ? sdi[tid] : 0.f;
     }
     if (tid == 0) acc.flush(st);
+    // smallest and largest |d| of the block, by the first warp
+    if (warp == 0) {
+        double lo = DBL_MAX, hi = 0.0;
+        for (int k = lane; k < nb; k += 32) {
+            const double a = fabs(sd64[k]);
+            lo = fmin(lo, a);
+            hi = fmax(hi, a);
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+            hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+        }
+        if (lane == 0 && nb > 0) {
+            atomicMin(&st->min_bits, (unsigned long long)__double_as_longlong(lo));
+            atomicMax(&st->max_bits, (unsigned long long)__double_as_longlong(hi));
+        }
+    }
 }
 
 // 4-byte asynchronous copy global -> shared (zero fill when !valid: nothing is read then).
