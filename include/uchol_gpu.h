@@ -103,6 +103,11 @@ typedef struct {
                                            diagonal block's unit-lower triangle (built after each
                                            factorisation), so that their triangular solves are products
                                            instead of a chain of block solves.  0 = 2048, < 0 = off. */
+    int64_t device_memory_budget;       /* > 0: a factorisation whose factor, contribution arena, staging,
+                                           inverses and value copies (uchol_estimate_device_bytes) exceed
+                                           this many bytes fails with UCHOL_OOM before any of it is
+                                           allocated; 0 = no budget.  The reference's counterpart is its
+                                           EstimatePeakBytes (UtduSymbolicFactorization.cs:203-219). */
 } uchol_options;
 
 /* Pivot statistics (UtduNumericFactorization.cs:57-84) and timings. */
@@ -212,6 +217,8 @@ int uchol_autotune(uchol_symbolic s, int n, int nnz, const double* values, const
  * the host from the symbolic arrays alone (no GPU needed): factor panels,
  * the planned contribution arena and the tensor-core operand staging (with
  * the K-split workspace of the tensor-core updates, 40 MB for a 152-SM GPU).
+ * With opts->device_memory_budget > 0 it returns UCHOL_OOM when the whole
+ * reservation (also the inverses and the value copies) exceeds the budget.
  * Counterpart of UtduSymbolicFactorization.EstimatePeakBytes
  * (CAESolvers/UCHOL/UtduSymbolicFactorization.cs:203-219). */
 int uchol_estimate_device_bytes(const uchol_symbolic_desc* desc, const uchol_options* opts, int64_t* factor_bytes,
@@ -230,7 +237,8 @@ int uchol_estimate_device_bytes(const uchol_symbolic_desc* desc, const uchol_opt
  * exit): n * nrhs + 128 * nrhs must not exceed 2^20 and nrhs must not exceed
  * 64, otherwise UCHOL_BAD_ARG.  The first call on a device looks up the
  * array's device address (cudaGetSymbolAddress), so make that first call
- * before any stream capture.  All calls share the array: calls that overlap
+ * before any stream capture; so is the first call after a device reset or
+ * under another context, which looks the address up again.  All calls share the array: calls that overlap
  * on the GPU (other streams, other threads) race and must be serialised by
  * the caller.  Work is queued on `stream` (cudaStream_t, NULL = default);
  * results are valid once that stream has completed.  The mirrored half of
@@ -240,6 +248,20 @@ int uchol_residual_norms_static(int n, int nnz, int nrhs, const int* d_row_ptr, 
                                 const double* d_values, const double* d_b, int ldb, const double* d_x, int ldx,
                                 double* d_norms, void* stream);
 const char* uchol_residual_norms_static_error(void);
+
+/* Bounded waits of the kernels, in milliseconds, on the current device: waits of the
+ * triangular solves (default 1000) and of the tensor-core Schur update (default 2000);
+ * a value <= 0 restores the default.  An expired wait makes the call report UCHOL_TIMEOUT
+ * with the device context still usable.  No counterpart in the reference (CPU threads). */
+int uchol_set_wait_limits(double solve_ms, double factor_ms);
+
+/* Failure check of the bounded waits: runs the factor's first level-solve launch (forward)
+ * whose front has at least three diagonal blocks with its bulk CTAs withheld, so that a
+ * chain waits on a progress counter that is never published, under a solve wait limit of
+ * wait_ms.  Returns UCHOL_TIMEOUT when the wait expired, as designed, and leaves the factor
+ * usable; UCHOL_BAD_ARG when the factor has no such launch (use inverse_block_width < 0 and
+ * a front wider than three solve blocks).  No counterpart in the reference. */
+int uchol_check_solve_wait(uchol_factor f, double wait_ms);
 
 /* Kernel checks: one launch of a factorisation kernel of the mixed path on caller data
  * (host buffers), so that tests can compare each kernel with an FP64 computation on the

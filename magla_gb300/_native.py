@@ -63,7 +63,7 @@ class Options(C.Structure):
         ("allow_diagonal_regularization", C.c_int), ("pivot_tolerance", C.c_double),
         ("diagonal_regularization", C.c_double), ("panel_width", C.c_int), ("precision", C.c_int),
         ("block_width", C.c_int), ("small_front_buckets", C.c_int), ("chain_merge_width", C.c_int),
-        ("inverse_block_width", C.c_int),
+        ("inverse_block_width", C.c_int), ("device_memory_budget", C.c_int64),
     ]
 
 
@@ -158,6 +158,8 @@ GPU_SYMBOLS = {
                                            C.POINTER(C.c_int64), c_int_p]),
     "uchol_check_diag_panel": (C.c_int, [C.c_int, C.c_int, C.c_void_p, C.c_double, C.c_double, C.c_int, C.c_void_p,
                                          C.c_void_p, C.c_void_p, c_int_p]),
+    "uchol_set_wait_limits": (C.c_int, [C.c_double, C.c_double]),
+    "uchol_check_solve_wait": (C.c_int, [C.c_void_p, C.c_double]),
     "uchol_kernel_launches": (C.c_int64, []),
     "uchol_set_phase_timing": (None, [C.c_int]),
     "uchol_last_error": (C.c_char_p, []),

@@ -120,6 +120,27 @@ struct DevPlan {
     DBuf rows, child_ptr, children;   // structure of the device fronts
 };
 
+// Device memory a factor of this plan reserves when it is created (the solve workspace,
+// which depends on the number of right-hand sides, comes on top).
+int64_t planned_bytes(const Plan& P, int precision, long long nnz, long long full_nnz, int n) {
+    const int64_t elem = precision == UCHOL_PRECISION_FP64 ? 8 : 4;
+    const int64_t op = precision == UCHOL_PRECISION_BF16 ? 2 : 4;
+    const int64_t sb = P.cfg.solve_block;
+    int64_t b = (P.factor_elems + P.contrib_elems) * elem;
+    if (P.cfg.tensor_core)
+        b += 2 * P.stage_elems * op + (int64_t)std::max(1, P.diag_slots) * kMinvStride * 4 +
+             (int64_t)tc_ws_floats(152) * 4 + (int64_t)tc_counter_count(152) * 4;
+    b += ((int64_t)P.inv_blocks.size() + P.inv_off_blocks) * sb * sb * elem;
+    b += (nnz + full_nnz) * 8 + (int64_t)n * 8;
+    return b;
+}
+
+void check_budget(int64_t budget, int64_t need) {
+    if (budget > 0 && need > budget)
+        throw Error(UCHOL_OOM, "the factorisation needs " + std::to_string(need) + " bytes of device memory, more than "
+                                   "the budget of " + std::to_string(budget) + " bytes");
+}
+
 inline int grid_for(long long work, int block, int cap = 152 * 16) {
     long long g = (work + block - 1) / block;
     return (int)std::max<long long>(1, std::min<long long>(g, cap));
@@ -143,13 +164,18 @@ struct uchol_symbolic_s {
     std::map<std::string, std::unique_ptr<DevPlan>> plans;
     std::mutex mu;
 
-    DevPlan* get_plan(const PlanConfig& c) {
+    // The plan of a configuration, built once and uploaded; `budget` > 0 rejects a plan whose
+    // factor would need more device memory (UCHOL_OOM) before anything is uploaded.
+    DevPlan* get_plan(const PlanConfig& c, int precision = UCHOL_PRECISION_FP64, int64_t budget = 0) {
         std::string key = std::to_string(c.pivot_block) + "/" + std::to_string(c.outer_block) + "/" +
                           std::to_string(c.small_mask) + "/" + std::to_string(c.tensor_core) + "/" +
                           std::to_string(c.solve_block) + "/" + std::to_string(c.merge_cols) + "/" +
                           std::to_string(c.merge_fill) + "/" + std::to_string(c.inv_cols);
         auto it = plans.find(key);
-        if (it != plans.end()) return it->second.get();
+        if (it != plans.end()) {
+            check_budget(budget, planned_bytes(it->second->plan, precision, nnz, full_nnz, n));
+            return it->second.get();
+        }
         auto dp = std::make_unique<DevPlan>();
         try {
             dp->plan = build_plan(n, count, first_col.data(), parent.data(), child_ptr.data(), children.data(),
@@ -159,6 +185,7 @@ struct uchol_symbolic_s {
             throw Error(UCHOL_BAD_ARG, std::string("inconsistent symbolic factorization: ") + e.what());
         }
         const Plan& P = dp->plan;
+        check_budget(budget, planned_bytes(P, precision, nnz, full_nnz, n));
         dp->sn.upload(P.sn, stream, "supernode table");
         dp->rel.upload(P.rel, stream, "relative indices");
         dp->asm_pos.upload(P.assemble_pos, stream, "assembly map");
@@ -609,6 +636,7 @@ void check_options(const uchol_options* o) {
         throw Error(UCHOL_BAD_ARG, "unknown precision mode");
     if (!(o->pivot_tolerance >= 0.0) || !(o->diagonal_regularization > 0.0))
         throw Error(UCHOL_BAD_ARG, "pivot tolerance must be >= 0 and regularization > 0");
+    if (o->device_memory_budget < 0) throw Error(UCHOL_BAD_ARG, "the device memory budget must be >= 0");
     if (o->small_front_buckets < 0 || o->small_front_buckets >= (1 << kSmallBuckets))
         throw Error(UCHOL_BAD_ARG, "small_front_buckets has bits beyond the " + std::to_string(kSmallBuckets) +
                                        " front-size buckets");
@@ -633,7 +661,7 @@ uchol_factor_s* create_factor(uchol_symbolic_s* S, int n, int nnz, const uchol_o
     F->precision = F->opts.precision;
     F->elem = F->precision == UCHOL_PRECISION_FP64 ? 8 : 4;
     PlanConfig cfg = config_for(F->opts);
-    F->dp = S->get_plan(cfg);
+    F->dp = S->get_plan(cfg, F->precision, F->opts.device_memory_budget);
     const Plan& P = F->dp->plan;
     cudaStream_t st = S->stream;
     F->panel.alloc((size_t)P.factor_elems * F->elem, "factor panels");
@@ -743,11 +771,8 @@ struct SolveTimer {
     }
 };
 
-template <class T, class Cv, int SB, int RG>
-void run_solve(uchol_factor_s* F, int nrhs, Cv* work, Cv* fv, Cv* fv2, cudaStream_t st, SolveTimer* timer = nullptr) {
-    uchol_symbolic_s* S = F->sym;
+SolveArgs solve_args(uchol_factor_s* F, int nrhs) {
     DevPlan& D = *F->dp;
-    const Plan& P = D.plan;
     SolveArgs A;
     A.sn = D.sn.as<SnDev>();
     A.rel = D.rel.as<int>();
@@ -755,10 +780,19 @@ void run_solve(uchol_factor_s* F, int nrhs, Cv* work, Cv* fv, Cv* fv2, cudaStrea
     A.child_ptr = D.child_ptr.as<int>();
     A.children = D.children.as<int>();
     A.fvec_off = D.fvec_off.as<long long>();
-    A.fv_stride = P.fvec_elems;
-    A.n = S->n;
+    A.fv_stride = D.plan.fvec_elems;
+    A.n = F->sym->n;
     A.nrhs = nrhs;
-    A.ldw = S->n;
+    A.ldw = F->sym->n;
+    return A;
+}
+
+// RG: right-hand sides the level kernels and the backward column dots carry together.
+template <class T, class Cv, int SB, int RG>
+void run_solve(uchol_factor_s* F, int nrhs, Cv* work, Cv* fv, Cv* fv2, cudaStream_t st, SolveTimer* timer = nullptr) {
+    DevPlan& D = *F->dp;
+    const Plan& P = D.plan;
+    const SolveArgs A = solve_args(F, nrhs);
     const T* panel = F->panel.as<T>();
     const Cv* linv = F->linv.as<Cv>();
     const SolveBlockTask* tasks = D.solve_tasks.as<SolveBlockTask>();
@@ -980,6 +1014,55 @@ void launch_solve_graph(uchol_factor_s* F, int nrhs, Cv* work, cudaStream_t st) 
     counted(F->solve_graph_nodes);
 }
 
+void ensure_workspace(uchol_factor_s* F, int nrhs);
+
+// Failure check of the bounded waits: the plan's first forward level launch whose front has
+// three or more diagonal blocks, with every CTA a chain CTA, so that the chains' waits for the
+// bulk CTAs' progress counters can only expire.  The solve set-up (workspace, tile maps, flags,
+// kernel attributes) is that of a one-column solve, made first.
+template <class T, class Cv, int SB>
+void starved_level_launch(uchol_factor_s* F, cudaStream_t st) {
+    DevPlan& D = *F->dp;
+    const Plan& P = D.plan;
+    const SolveLaunch* Lp = nullptr;
+    for (const SolveLaunch& L : P.fwd_launches)
+        if (L.kind == SolveLaunch::FwdLevel && L.steps >= 3 && L.count > 0) {
+            Lp = &L;
+            break;
+        }
+    if (!Lp)
+        throw Error(UCHOL_BAD_ARG, "the factor has no level-solve launch with a chain of three diagonal blocks "
+                                   "(use inverse_block_width < 0 and a front wider than three solve blocks)");
+    ensure_workspace(F, 1);
+    CK(cudaMemsetAsync(F->work.p, 0, F->work.bytes, st));
+    launch_solve_graph<T, Cv, SB>(F, 1, F->work.as<Cv>(), st);   // set-up, and a normal solve of zeros
+    CK(cudaStreamSynchronize(st));
+    const SolveBlockTask* tasks = D.solve_tasks.as<SolveBlockTask>();
+    const int nblocks = (int)P.inv_blocks.size();
+    int* fwd_flags = F->solve_flags.as<int>();
+    int* progress = fwd_flags + 2 * nblocks;
+    CK(cudaMemsetAsync(fwd_flags, 0, sizeof(int) * ((size_t)2 * nblocks + P.progress_count), st));
+    const int grid = std::max(1, std::min(Lp->count, F->coop_fwd));
+    LevelArgs la;
+    la.chains = tasks + Lp->begin;
+    la.nchains = Lp->count;
+    la.bulk = tasks + Lp->bulk_begin;
+    la.nbulk = Lp->bulk_count;
+    la.nchain_cta = grid;   // no bulk CTA: the progress counters never move
+    la.ndiag = Lp->ndiag;
+    la.ndiag_cta = 0;
+    la.steps = Lp->steps;
+    la.flags = fwd_flags;
+    la.progress = progress + Lp->progress_off;
+    la.status = F->solve_status.as<int>();
+    la.maps = F->solve_maps.as<CUtensorMap>();
+    launch_cooperative(k_fwd_level<T, Cv, SB, 1>, grid, 256, level_smem_bytes<T, Cv, SB, 1>(), st, la,
+                       solve_args(F, 1), F->panel.as<T>(), F->linv.as<Cv>(), F->fv.as<Cv>(), F->fv2.as<Cv>(),
+                       F->diag.as<double>(), F->work.as<Cv>());
+    counted();
+    CK(cudaStreamSynchronize(st));
+}
+
 void ensure_workspace(uchol_factor_s* F, int nrhs) {
     if (F->ws_nrhs >= nrhs) return;
     uchol_symbolic_s* S = F->sym;
@@ -1156,6 +1239,38 @@ int64_t uchol_kernel_launches(void) { return g_launches.load(); }
 
 void uchol_set_phase_timing(int on) { g_phase_timing.store(on ? 1 : 0); }
 
+int uchol_set_wait_limits(double solve_ms, double factor_ms) {
+    return guarded([&] {
+        const unsigned long long s = solve_ms > 0.0 ? (unsigned long long)(solve_ms * 1e6) : kDefaultSolveWaitNs;
+        const unsigned long long f = factor_ms > 0.0 ? (unsigned long long)(factor_ms * 1e6) : kDefaultFactorWaitNs;
+        CK(cudaMemcpyToSymbol(g_solve_wait_ns, &s, sizeof(s)));
+        CK(cudaMemcpyToSymbol(g_factor_wait_ns, &f, sizeof(f)));
+    });
+}
+
+int uchol_check_solve_wait(uchol_factor f, double wait_ms) {
+    return guarded([&] {
+        if (!f) throw Error(UCHOL_BAD_ARG, "factor handle is null");
+        if (!(wait_ms > 0.0)) throw Error(UCHOL_BAD_ARG, "the wait limit must be positive");
+        std::lock_guard<std::mutex> lk(f->mu);
+        cudaStream_t st = f->sym->stream;
+        unsigned long long old = kDefaultSolveWaitNs;
+        CK(cudaMemcpyFromSymbol(&old, g_solve_wait_ns, sizeof(old)));
+        const unsigned long long lim = (unsigned long long)(wait_ms * 1e6);
+        CK(cudaMemcpyToSymbol(g_solve_wait_ns, &lim, sizeof(lim)));
+        try {
+            if (f->precision == UCHOL_PRECISION_FP64) starved_level_launch<double, double, 64>(f, st);
+            else starved_level_launch<float, float, 128>(f, st);
+        } catch (...) {
+            cudaMemcpyToSymbol(g_solve_wait_ns, &old, sizeof(old));
+            throw;
+        }
+        CK(cudaMemcpyToSymbol(g_solve_wait_ns, &old, sizeof(old)));
+        check_solve_status(f);   // UCHOL_TIMEOUT when the wait expired, status cleared
+        throw Error(UCHOL_INTERNAL, "the starved level solve completed: its wait did not expire");
+    });
+}
+
 void uchol_default_options(uchol_options* o) {
     if (!o) return;
     o->allow_diagonal_regularization = 1;
@@ -1167,6 +1282,7 @@ void uchol_default_options(uchol_options* o) {
     o->small_front_buckets = 0;
     o->chain_merge_width = 0;
     o->inverse_block_width = 0;
+    o->device_memory_budget = 0;
 }
 
 int uchol_symbolic_create(const uchol_symbolic_desc* d, uchol_symbolic* out) {
@@ -1280,6 +1396,8 @@ int uchol_estimate_device_bytes(const uchol_symbolic_desc* d, const uchol_option
                                              : 0;
         if (levels) *levels = P.levels;
         if (launches) *launches = (int)P.launches.size();
+        const long long nnz = d->nnz;
+        check_budget(o.device_memory_budget, planned_bytes(P, o.precision, nnz, 2 * nnz - n, n));
     });
 }
 

@@ -7,6 +7,17 @@
 
 namespace uchol_dev {
 
+#ifdef __CUDACC__
+// Limits of the kernels' bounded waits, in ns (uchol_set_wait_limits changes them on the
+// current device): the solves' waits on flags, counters and copies, and the tensor-core
+// update's waits on its mbarriers.  On expiry a kernel records a status word and returns,
+// and the host call reports UCHOL_TIMEOUT.
+constexpr unsigned long long kDefaultSolveWaitNs = 1000000000ull;    // 1 s
+constexpr unsigned long long kDefaultFactorWaitNs = 2000000000ull;   // 2 s
+static __device__ unsigned long long g_solve_wait_ns = kDefaultSolveWaitNs;
+static __device__ unsigned long long g_factor_wait_ns = kDefaultFactorWaitNs;
+#endif
+
 // Front of one supernode.  Rows are local indices 0..m-1 (the supernode's
 // sorted row pattern); columns 0..w-1 are the pivots.  Storage is split in
 // two column-major pieces:

@@ -164,7 +164,6 @@ __global__ void __launch_bounds__(SB) k_invert_blocks(const SolveBlockTask* __re
 // Everything proceeds step-major: a wait at step b is only ever for a flag
 // or counter of step b-1, so no CTA can block its own producer.
 
-constexpr unsigned long long kSolveWaitNs = 1000000000ull;   // 1 s per bounded wait
 constexpr size_t kLevelSmemSlack = 1024;                      // alignment slack of the level kernels' dynamic smem
 constexpr int kSolveRhsGroup = 16;                            // right-hand sides per group of the multi-column solves
 constexpr int kSolveStatusTimeout = 2;
@@ -216,7 +215,7 @@ __device__ __forceinline__ bool bar_wait(unsigned long long* bar, unsigned parit
     const unsigned long long t0 = solve_ns();
     for (;;) {
         if (bar_try(bar, parity)) return true;
-        if (solve_ns() - t0 > kSolveWaitNs) {
+        if (solve_ns() - t0 > g_solve_wait_ns) {
             atomicExch(status, kSolveStatusTimeout);
             return false;
         }
@@ -245,7 +244,7 @@ __device__ __forceinline__ void start_tile_copy(T* Tl, Cv* Li, const CUtensorMap
     bulk_g2s(Li, inv, inv_bytes, bar);
 }
 
-// Thread 0 waits for *flag >= target, giving up after kSolveWaitNs (status :=
+// Thread 0 waits for *flag >= target, giving up after g_solve_wait_ns (status :=
 // timeout) or as soon as another CTA has given up; the CTA learns the outcome.
 __device__ __forceinline__ bool wait_at_least(const int* flag, int target, int* status, int* ok) {
     if (threadIdx.x == 0) {
@@ -261,7 +260,7 @@ __device__ __forceinline__ bool wait_at_least(const int* flag, int target, int* 
                     good = 0;
                     break;
                 }
-                if (solve_ns() - t0 > kSolveWaitNs) {
+                if (solve_ns() - t0 > g_solve_wait_ns) {
                     atomicExch(status, kSolveStatusTimeout);
                     good = 0;
                     break;

@@ -8,6 +8,7 @@
 // file offers the FP64 residual check of uchol_residual_norms with every
 // buffer supplied by the caller and the only scratch in a fixed-size array
 // that the library declares statically on every device that loads it.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -28,6 +29,7 @@ static __device__ __align__(256) double g_residual_scratch[kScratchDoubles];
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
 double* g_scratch_ptr[kMaxDevices] = {nullptr};
+CUcontext g_scratch_ctx[kMaxDevices] = {nullptr};   // the context each cached address belongs to
 thread_local std::string g_static_error;
 
 struct Fail {
@@ -87,20 +89,43 @@ __global__ void k_residual_finish(const double* __restrict__ partial, int blocks
     out[j] = sqrt(s);
 }
 
-// Host address of the static array on the current device, looked up once per device.
+// The driver's cuCtxGetCurrent, through the runtime (the library links no driver library).
+CUresult current_context(CUcontext* ctx) {
+    using Fn = CUresult (*)(CUcontext*);
+    static Fn fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess || !p)
+            return CUDA_ERROR_NOT_FOUND;
+        fn = reinterpret_cast<Fn>(p);
+    }
+    return fn(ctx);
+}
+
+// Device address of the static array on the current device, looked up once per device and
+// context: after a device reset (or under another context) the module is loaded anew and
+// the address is looked up again.
 double* scratch_on_current_device() {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) throw Fail{UCHOL_CUDA_ERROR, std::string("cudaGetDevice failed: ") + cudaGetErrorString(e)};
     if (dev < 0 || dev >= kMaxDevices) throw Fail{UCHOL_BAD_ARG, "device ordinal out of range"};
+    // no context is current yet on a thread that has made no CUDA call: then the lookup below
+    // (which makes the device's primary context current) runs, and the context is read after it
+    CUcontext ctx = nullptr;
+    if (current_context(&ctx) != CUDA_SUCCESS) throw Fail{UCHOL_CUDA_ERROR, "cuCtxGetCurrent failed"};
     std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_scratch_ptr[dev]) {
+    if (!ctx || !g_scratch_ptr[dev] || g_scratch_ctx[dev] != ctx) {
         void* p = nullptr;
         e = cudaGetSymbolAddress(&p, g_residual_scratch);
         if (e != cudaSuccess || !p)
             throw Fail{UCHOL_CUDA_ERROR,
                        std::string("cudaGetSymbolAddress of the static scratch failed: ") + cudaGetErrorString(e)};
+        if (current_context(&ctx) != CUDA_SUCCESS || !ctx) throw Fail{UCHOL_CUDA_ERROR, "no current CUDA context"};
         g_scratch_ptr[dev] = static_cast<double*>(p);
+        g_scratch_ctx[dev] = ctx;
     }
     return g_scratch_ptr[dev];
 }

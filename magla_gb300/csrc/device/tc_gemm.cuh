@@ -34,7 +34,6 @@
 
 namespace uchol_dev {
 
-constexpr unsigned long long kWaitLimitNs = 2000000000ull;  // 2 s per bounded wait
 constexpr int kTcStatusTimeout = 1;
 
 // ---------------------------------------------------------------- PTX helpers
@@ -70,9 +69,10 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
     return ok != 0;
 }
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-    const unsigned long long t0 = global_ns();
+    if (mbar_try_wait(bar, parity)) return true;
+    const unsigned long long t0 = global_ns(), limit = g_factor_wait_ns;
     while (!mbar_try_wait(bar, parity))
-        if (global_ns() - t0 > kWaitLimitNs) return false;
+        if (global_ns() - t0 > limit) return false;
     return true;
 }
 

@@ -59,6 +59,7 @@ class UtduSolverOptions:
         self.SmallFrontBuckets = 0   # bit b: fronts of 32b < m <= 32(b+1) rows go whole to one CTA (0 = 0x7)
         self.ChainMergeWidth = 0     # widest device front grouped from a chain of supernodes (0 = 1024, < 0 = off)
         self.InverseBlockWidth = 0   # widest front whose diagonal block is kept inverted for the solves (0 = 2048, < 0 = off)
+        self.DeviceMemoryBudget = 0  # bytes; > 0: factorisations needing more fail with OOM before allocating
         self.RefinementTolerance = 1e-12
         self.RefinementMaxIterations = 50
         for k, v in kw.items():
@@ -84,6 +85,7 @@ class UtduSolverOptions:
         o.small_front_buckets = int(self.SmallFrontBuckets)
         o.chain_merge_width = int(self.ChainMergeWidth)
         o.inverse_block_width = int(self.InverseBlockWidth)
+        o.device_memory_budget = int(self.DeviceMemoryBudget)
         return o
 
 
