@@ -62,6 +62,9 @@ def parse():
     p.add_argument("--nrhs", type=int, default=16, help="right-hand sides per solve")
     p.add_argument("--perturbations", type=int, default=10,
                    help="value sets with E = 1 + uniform[-0.05, 0.05] per element (0: E = 1 throughout)")
+    p.add_argument("--contrast", type=float, default=1.0,
+                   help="> 1: Young's modulus log-uniform in [1, contrast] per element (seeded), the "
+                        "stiffness-contrast elasticity case (1e4)")
     p.add_argument("--tol", type=float, default=1e-10)
     p.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 GPU arm")
     p.add_argument("--cpu-sample-elements", type=int, nargs=3, default=None,
@@ -130,11 +133,13 @@ def make_workload(args):
     from magla_gb300 import generators as G
     ex, ey, ez = args.elements
     rng = np.random.default_rng(20260812)
+    base = (G.log_uniform_youngs(ex * ey * ez, 1.0, args.contrast, np.random.default_rng(20260813))
+            if args.contrast > 1.0 else np.ones(ex * ey * ez))
     sets = []
     if args.perturbations > 0:
         m = load = None
         for k in range(args.perturbations):
-            E = 1.0 + rng.uniform(-0.05, 0.05, ex * ey * ez)
+            E = base * (1.0 + rng.uniform(-0.05, 0.05, ex * ey * ez))
             mk, lk = G.elasticity(ex, ey, ez, youngs=E)
             if m is None:
                 m, load = mk, lk
@@ -142,7 +147,7 @@ def make_workload(args):
                 raise RuntimeError("a value perturbation changed the sparsity pattern")
             sets.append(np.ascontiguousarray(mk.Values))
     else:
-        m, load = G.elasticity(ex, ey, ez)
+        m, load = G.elasticity(ex, ey, ez, youngs=base if args.contrast > 1.0 else None)
         sets.append(np.ascontiguousarray(m.Values))
     # n x nrhs block (column-major): unit body force plus uniform[-0.1, 0.1] noise per column
     b = np.asfortranarray(np.stack([load + rng.uniform(-0.1, 0.1, m.Size) for _ in range(args.nrhs)], axis=1))
@@ -331,7 +336,9 @@ def run_ours(args):
         "config": {"workload": f"elasticity Q1 {args.elements[0]}x{args.elements[1]}x{args.elements[2]} elements, "
                                f"n={m.Size}, nnz_upper={m.NonZeroCount}, {args.ordering} ordering, {nrhs} right-hand "
                                f"sides, {max(1, args.perturbations)} value sets"
-                               + (" (E x (1 + uniform[-0.05, 0.05]) per element)" if args.perturbations else ""),
+                               + (" (E x (1 + uniform[-0.05, 0.05]) per element)" if args.perturbations else "")
+                               + (f", E log-uniform in [1, {args.contrast:g}] per element" if args.contrast > 1.0
+                                  else ""),
                    "precision": (f"{prec.name} Schur GEMMs (FP32 accumulation), FP32 fronts, FP64-residual refinement"
                                  if prec != mg.Precision.FP64 else "FP64 throughout"),
                    "refine_tol": args.tol, "factor_ops": ops, "parallelism": f"replicas{world}", "nrhs": nrhs,

@@ -397,8 +397,17 @@ __device__ __forceinline__ void store_op4(__nv_bfloat16* p, float a, float b, fl
     v.y = *reinterpret_cast<unsigned*>(&hi);
     *reinterpret_cast<uint2*>(p) = v;
 }
+// TF32 operands: rounded to TF32 precision (nearest, ties away) as they are staged, so that
+// the tensor core, which reads only the top 19 bits of each FP32 operand, multiplies rounded
+// rather than truncated values (truncation biases every product the same way, and over the
+// many updates of a deep tree that bias accumulates in the factor).
+__device__ __forceinline__ float round_tf32(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return __uint_as_float(r);
+}
 __device__ __forceinline__ void store_op4(float* p, float a, float b, float c, float e) {
-    *reinterpret_cast<float4*>(p) = make_float4(a, b, c, e);
+    *reinterpret_cast<float4*>(p) = make_float4(round_tf32(a), round_tf32(b), round_tf32(c), round_tf32(e));
 }
 __device__ __forceinline__ void store_op1(__nv_bfloat16* p, float a) { *p = __float2bfloat16_rn(a); }
 __device__ __forceinline__ void store_op1(float* p, float a) { *p = a; }
