@@ -129,7 +129,7 @@ GPU_SYMBOLS = {
     "uchol_symbolic_create": (C.c_int, [C.POINTER(SymbolicDesc), c_void_pp]),
     "uchol_symbolic_destroy": (C.c_int, [C.c_void_p]),
     "uchol_symbolic_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
-    "uchol_factorize": (C.c_int, [C.c_void_p, C.c_int, C.c_int, c_double_p, C.POINTER(Options), c_void_pp,
+    "uchol_factorize": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.POINTER(Options), c_void_pp,
                                   C.POINTER(FactorStats)]),
     "uchol_factorize_device": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.POINTER(Options), c_void_pp,
                                          C.POINTER(FactorStats)]),

@@ -60,6 +60,9 @@ class UtduSolverOptions:
         self.ChainMergeWidth = 0     # widest device front grouped from a chain of supernodes (0 = 1024, < 0 = off)
         self.InverseBlockWidth = 0   # widest front whose diagonal block is kept inverted for the solves (0 = 2048, < 0 = off)
         self.DeviceMemoryBudget = 0  # bytes; > 0: factorisations needing more fail with OOM before allocating
+        # reduced precision breaks down (a pivot regularised or not finite): factorise again in the
+        # next higher precision, BF16 -> TF32 -> FP64
+        self.PrecisionFallback = True
         self.RefinementTolerance = 1e-12
         self.RefinementMaxIterations = 50
         for k, v in kw.items():
@@ -293,6 +296,7 @@ class UtduNumericFactorization:
         self._nnz = matrix.NonZeroCount
         self._diag = None
         self.LastRefinement = None
+        self.PrecisionFallbackFrom = []   # precisions given up before this factor's (PrecisionFallback)
 
     @property
     def Symbolic(self) -> UtduSymbolicFactorization:
@@ -511,16 +515,46 @@ class SymmetricUtduSolver(DirectLinearSolver):
             symbolic = self.Analyze(matrix)
         else:
             symbolic.EnsureCompatible(matrix)
+        vals = np.ascontiguousarray(matrix.Values, np.float64)
+        return self._factorize_with_fallback(matrix, symbolic, vals.ctypes.data, False)
+
+    @staticmethod
+    def _broke_down(stats) -> bool:
+        """A reduced-precision factor is unusable when a pivot was regularised (the low-precision
+        Schur complement lost definiteness) or a pivot is not finite."""
+        return (stats.regularized_pivot_count > 0 or not np.isfinite(stats.smallest_pivot_magnitude)
+                or not np.isfinite(stats.largest_pivot_magnitude))
+
+    def _factorize_with_fallback(self, matrix, symbolic, values_ptr, on_device):
+        """uchol_factorize[_device] in the options' precision; when PrecisionFallback is set and a
+        reduced-precision factor breaks down, again in the next higher precision (the returned
+        factor's ``PrecisionFallbackFrom`` lists the precisions given up).  A factor that keeps
+        regularised pivots in FP64 is the reference's own result (a singular matrix)."""
         lib = _native.gpu()
         h = symbolic.device_handle()
-        out = C.c_void_p()
-        stats = _native.FactorStats()
-        opts = self.Options._native_options()
-        vals = np.ascontiguousarray(matrix.Values, np.float64)
-        st = lib.uchol_factorize(h, matrix.Size, matrix.NonZeroCount, _native.ptr(vals, C.c_double), C.byref(opts),
-                                 C.byref(out), C.byref(stats))
-        raise_for_status(st, lib.uchol_last_error())
-        return UtduNumericFactorization(symbolic, out, stats, self.Options, matrix)
+        order = [Precision.BF16, Precision.TF32, Precision.FP64]
+        options = self.Options
+        given_up = []
+        while True:
+            out = C.c_void_p()
+            stats = _native.FactorStats()
+            opts = options._native_options()
+            fn = lib.uchol_factorize_device if on_device else lib.uchol_factorize
+            st = fn(h, matrix.Size, matrix.NonZeroCount, C.c_void_p(values_ptr), C.byref(opts), C.byref(out),
+                    C.byref(stats))
+            p = Precision(options.Precision)
+            fall = (options.PrecisionFallback and p != Precision.FP64 and
+                    (st == _native.NOT_SPD or (st == _native.OK and self._broke_down(stats))))
+            if not fall:
+                raise_for_status(st, lib.uchol_last_error())
+                f = UtduNumericFactorization(symbolic, out, stats, options, matrix)
+                f.PrecisionFallbackFrom = given_up
+                return f
+            if st == _native.OK:
+                lib.uchol_factor_destroy(out)
+            given_up.append(p)
+            options = copy.copy(options)
+            options.Precision = order[order.index(p) + 1]
 
     def FactorizeDevice(self, matrix: SymmetricCSRMatrix, symbolic: UtduSymbolicFactorization, d_values: int):
         """Factorize with the values already in device memory (pointer as an integer, the
@@ -528,14 +562,7 @@ class SymmetricUtduSolver(DirectLinearSolver):
         if matrix is None or symbolic is None:
             raise ArgumentNullException("matrix" if matrix is None else "symbolic")
         symbolic.EnsureCompatible(matrix)
-        lib = _native.gpu()
-        out = C.c_void_p()
-        stats = _native.FactorStats()
-        opts = self.Options._native_options()
-        st = lib.uchol_factorize_device(symbolic.device_handle(), matrix.Size, matrix.NonZeroCount,
-                                        C.c_void_p(d_values), C.byref(opts), C.byref(out), C.byref(stats))
-        raise_for_status(st, lib.uchol_last_error())
-        return UtduNumericFactorization(symbolic, out, stats, self.Options, matrix)
+        return self._factorize_with_fallback(matrix, symbolic, d_values, True)
 
     def SolveCore(self, matrix, right_hand_side):
         return self.Factorize(matrix).Solve(right_hand_side)

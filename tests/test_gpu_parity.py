@@ -226,12 +226,30 @@ def test_mixed_pivot_counts_match_the_fp64_path(gpu_lib, precision, fixture):
     negative counts as the FP64 oracle.  Bucket mask 0x10 sends these small fronts to the blocked
     kernels (k_diag_block) instead of the whole-front FP64 kernel."""
     m = fixture()
-    f = solver(Precision=precision, SmallFrontBuckets=0x10).Factorize(m)
+    f = solver(Precision=precision, SmallFrontBuckets=0x10, PrecisionFallback=False).Factorize(m)
+    assert f.Precision == precision
     sym, of = oracle_for(m)
     assert f.RegularizedPivotCount == of.RegularizedPivotCount
     assert f.NegativePivotCount == of.NegativePivotCount
     with pytest.raises(InvalidOperationException):
-        solver(Precision=precision, SmallFrontBuckets=0x10, AllowDiagonalRegularization=False).Factorize(m)
+        solver(Precision=precision, SmallFrontBuckets=0x10, AllowDiagonalRegularization=False,
+               PrecisionFallback=False).Factorize(m)
+
+
+@pytest.mark.parametrize("fixture", [F.singular, F.indefinite])
+def test_precision_fallback_ends_at_fp64_for_a_singular_matrix(gpu_lib, fixture):
+    """A reduced-precision factor with a regularised pivot is factorised again in the next
+    precision; a matrix that is singular in FP64 too ends with the reference's FP64 result."""
+    m = fixture()
+    f = solver(Precision=Precision.BF16, SmallFrontBuckets=0x10).Factorize(m)
+    assert f.Precision == Precision.FP64
+    assert f.PrecisionFallbackFrom == [Precision.BF16, Precision.TF32]
+    sym, of = oracle_for(m)
+    assert f.RegularizedPivotCount == of.RegularizedPivotCount
+    assert f.NegativePivotCount == of.NegativePivotCount
+    # an SPD matrix keeps the precision it asked for
+    g = solver(Precision=Precision.BF16).Factorize(G.grid_matrix(8, 8, 8, 2))
+    assert g.Precision == Precision.BF16 and g.PrecisionFallbackFrom == []
 
 
 def test_run_twice_is_bitwise_deterministic(gpu_lib):
