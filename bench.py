@@ -384,11 +384,12 @@ def _with_values(m, values):
 
 
 def gemm_traffic(args, prec):
-    """DRAM bytes per k_tc_gemm launch (read + write) from the committed ncu capture of this
-    workload (elasticity 40^3, BF16, AMD); None for any other configuration."""
+    """DRAM bytes per k_tc_gemm launch (read + write) from the committed ncu capture of the
+    default workload (elasticity 80x80x40, TF32, natural order); None for any other one."""
     import magla_gb300 as mg
-    f = ROOT / "profiles" / "k_tc_gemm_dram_elasticity40_bf16.txt"
-    if list(args.elements) != [40, 40, 40] or prec != mg.Precision.BF16 or args.ordering != "AMD" or not f.exists():
+    f = ROOT / "profiles" / "k_tc_gemm_dram_elasticity80x80x40_tf32.txt"
+    if list(args.elements) != [80, 80, 40] or prec != mg.Precision.TF32 or args.ordering != "Natural" \
+            or not f.exists():
         return None
     for line in f.read_text().splitlines():
         if line.startswith("traffic_bytes_per_launch:"):

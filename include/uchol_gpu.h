@@ -51,6 +51,8 @@ extern "C" {
 #define UCHOL_NO_CONVERGENCE 8    /* refinement did not reach its tolerance */
 #define UCHOL_INTERNAL 9
 #endif
+#define UCHOL_OUT_OF_RANGE 10     /* IndexOutOfRangeException / ArgumentOutOfRangeException */
+#define UCHOL_NOT_IN_PATTERN 11   /* InvalidOperationException: position absent from the sparse structure */
 
 typedef struct uchol_symbolic_s* uchol_symbolic;
 typedef struct uchol_factor_s* uchol_factor;
@@ -108,6 +110,10 @@ typedef struct {
                                            this many bytes fails with UCHOL_OOM before any of it is
                                            allocated; 0 = no budget.  The reference's counterpart is its
                                            EstimatePeakBytes (UtduSymbolicFactorization.cs:203-219). */
+    int split_min_kblocks;              /* mixed paths: a tensor-core update launch with fewer tiles than SMs is
+                                           split in K (stream-K) only when its tiles have at least this many
+                                           128-byte K blocks; 0 = 8, < 0 = never split.  uchol_autotune picks
+                                           it. */
 } uchol_options;
 
 /* Pivot statistics (UtduNumericFactorization.cs:57-84) and timings. */
@@ -194,11 +200,13 @@ typedef struct {
 int uchol_factor_phase_times(uchol_factor f, uchol_phase_times* t);
 
 /* Autotuner: per front-size bucket, the kernel that factorises the fronts (one CTA with
- * the whole front in shared memory, or the blocked path), and on the mixed paths the
- * outer-block width (64 or 128 columns).  uchol_autotune times graph-replayed
+ * the whole front in shared memory, or the blocked path); on the mixed paths the
+ * outer-block width (64 or 128 columns); the widest device front grouped from a supernode
+ * chain (512, 1024, 2048 columns or none); and on the mixed paths the stream-K threshold of
+ * the tensor-core updates (4, 8, 16 K blocks or never).  uchol_autotune times graph-replayed
  * refactorisations of these values for each candidate: the default first, then one
  * bucket toggled at a time from the largest down, each change kept when it is faster,
- * then the other block width.  It writes the fastest options to *best (the base options
+ * then the other block width, the merge widths and the thresholds in the same way.  It writes the fastest options to *best (the base options
  * with small_front_buckets and block_width set) and a report.  Every candidate builds its
  * own factor (device memory of one factorisation at a time).  No counterpart in the
  * reference, which has one CPU kernel per operation; the device has several shapes and
@@ -209,6 +217,8 @@ typedef struct {
     double best_ms;              /* of the chosen configuration */
     int small_front_buckets;     /* chosen bucket mask */
     int block_width;             /* chosen outer-block width (mixed paths; 0 on the FP64 path) */
+    int chain_merge_width;       /* chosen chain_merge_width (0 = the default, 1024) */
+    int split_min_kblocks;       /* chosen split_min_kblocks (0 = the default, 8) */
 } uchol_autotune_report;
 int uchol_autotune(uchol_symbolic s, int n, int nnz, const double* values, const uchol_options* base,
                    uchol_options* best, uchol_autotune_report* report);
@@ -286,6 +296,90 @@ int uchol_check_schur_update(int bf16, int m, int w, int c0, int cend, int kbeg,
 int uchol_check_diag_panel(int m, int nb, const float* front, double threshold, double regularization,
                            int allow_regularization, float* l_out, double* d_out, float* w_stage_out,
                            int* counts_out);
+
+/* ---- Device-resident matrix values ------------------------------------
+ * A uchol_dmatrix holds a SymmetricCSRMatrix on the device: its upper-triangle
+ * structure (row_ptr [n+1], col [nnz], ascending columns, row <= col, as
+ * CAESolvers/SymmetricCSRMatrix.cs:373-390 exposes it) and its values [nnz].
+ * The values are refreshed on the device by the reference's container
+ * operations and fed to a refactorisation without a host round trip:
+ *   ClearValues   (SymmetricCSRMatrix.cs:113-116)  uchol_dmatrix_clear_values
+ *   AccumulateAt  (SymmetricCSRMatrix.cs:98-110)   uchol_accumulate over a planned item list
+ *   LineCross     (SymmetricCSRMatrix.cs:125-167)  uchol_line_cross over a planned index list
+ *   Multiply      (SymmetricCSRMatrix.cs:293-324)  uchol_dmatrix_multiply
+ * Work is queued on the handle's stream (`stream`, NULL = a stream of its own);
+ * entry points with on_device = 0 take host buffers and return after the stream
+ * has completed, those with on_device = 1 take device buffers and return at once.
+ * A plan resolves each listed position on the host once (the errors of the
+ * reference's calls are reported when it is built); applying it is a fixed set
+ * of launches whose results equal the reference's sequential calls bit for bit. */
+typedef struct uchol_dmatrix_s* uchol_dmatrix;
+typedef struct uchol_values_plan_s* uchol_values_plan;
+
+/* values: host array [nnz] or NULL (zeros).  UCHOL_BAD_ARG for a structure that is not
+ * an upper-triangle CSR with strictly ascending columns. */
+int uchol_dmatrix_create(int n, int nnz, const int* row_ptr, const int* col, const double* values, void* stream,
+                         uchol_dmatrix* out);
+int uchol_dmatrix_destroy(uchol_dmatrix m);
+int uchol_dmatrix_set_stream(uchol_dmatrix m, void* stream);
+/* The device array of the values (owned by the handle; valid until it is destroyed). */
+int uchol_dmatrix_values(uchol_dmatrix m, double** d_values);
+int uchol_dmatrix_set_values(uchol_dmatrix m, const double* values, int on_device);
+int uchol_dmatrix_get_values(uchol_dmatrix m, double* out, int on_device);
+int uchol_dmatrix_clear_values(uchol_dmatrix m);
+/* AccumulateAt(rows[i], cols[i], item_i) for i = 0..count-1, in order: positions are
+ * normalised to (min, max); UCHOL_OUT_OF_RANGE for an index outside [0, n)
+ * (IndexOutOfRangeException), UCHOL_NOT_IN_PATTERN for a position absent from the
+ * structure (InvalidOperationException).  Several items may name one position: it
+ * receives their values in list order. */
+int uchol_accumulate_plan_create(uchol_dmatrix m, int count, const int* rows, const int* cols,
+                                 uchol_values_plan* out);
+/* values[pos_i] += items[i] (items: count values, host or device). */
+int uchol_accumulate(uchol_dmatrix m, uchol_values_plan p, const double* items, int on_device);
+/* LineCross(rhs, prescribed[t], indices[t]) for t = 0..count-1, in order:
+ * UCHOL_OUT_OF_RANGE for an index outside [0, n) (ArgumentOutOfRangeException),
+ * UCHOL_NOT_IN_PATTERN for an index whose diagonal is absent. */
+int uchol_line_cross_plan_create(uchol_dmatrix m, int count, const int* indices, uchol_values_plan* out);
+/* rhs: nrhs columns of n (leading dimension ldr); prescribed: nrhs columns of count
+ * (leading dimension ldp), column j holding the values of rhs column j.  Every column
+ * receives what the list of calls does to one right-hand side of the matrix as it was
+ * before this call; the values are then those after the list.  nrhs = 0 changes the
+ * values only. */
+int uchol_line_cross(uchol_dmatrix m, uchol_values_plan p, double* rhs, int ldr, int nrhs, const double* prescribed,
+                     int ldp, int on_device);
+int uchol_values_plan_destroy(uchol_values_plan p);
+/* y = A x in FP64 (nrhs columns). */
+int uchol_dmatrix_multiply(uchol_dmatrix m, int nrhs, const double* x, int ldx, double* y, int ldy, int on_device);
+
+/* Jacobi-preconditioned conjugate gradients on the device
+ * (CAESolvers/CGGP/ConjugateGradientGaussPreSolver.cs:78-165, JacobiPreconditioner.cs:12-57):
+ * x0 = the initial guess or 0; stop when ||b - A x_k|| <= tolerance * ||b|| (||b|| = 0: 1);
+ * at most max_iterations steps (0: n).  Each column iterates on its own.  UCHOL_NOT_SPD for
+ * a diagonal entry that is zero, absent, not finite or within pivot_tolerance of zero (only
+ * when a step is needed) and for p^T A p <= 0; UCHOL_OUT_OF_RANGE for a negative tolerance
+ * or iteration limit.  Not converging is not an error: results[j].converged = 0. */
+typedef struct {
+    double relative_tolerance;   /* RelativeTolerance, default 1e-8 */
+    int max_iterations;          /* MaxIterations, default 0 (= n) */
+    int use_preconditioner;      /* UsePreconditioner, default 1 */
+    int use_initial_guess;       /* 1: x holds the initial guess on entry */
+    double pivot_tolerance;      /* JacobiPreconditioner pivotTolerance, default 1e-300 */
+} uchol_cg_options;
+typedef struct {
+    int iterations;
+    int converged;
+    double residual_norm;        /* ||b - A x|| of the iteration's recurrence */
+    double relative_residual;
+    double ms;                   /* whole call, device time */
+} uchol_cg_result;
+void uchol_default_cg_options(uchol_cg_options* o);
+int uchol_jacobi_pcg(uchol_dmatrix m, int nrhs, const double* b, int ldb, double* x, int ldx, int on_device,
+                     const uchol_cg_options* opts, uchol_cg_result* results);
+
+/* Refactorise f with the values of m (same structure as f's symbolic factorisation,
+ * else UCHOL_PATTERN_MISMATCH).  The factorisation's stream waits for the work queued on
+ * m's stream; the values do not leave the device. */
+int uchol_refactorize_dmatrix(uchol_factor f, uchol_dmatrix m, uchol_factor_stats* stats);
 
 /* Number of kernel launches this library has issued since it was loaded. */
 int64_t uchol_kernel_launches(void);

@@ -7,6 +7,8 @@ sm_103a.  See include/uchol_host.h and include/uchol_gpu.h for the C-ABI.
 from .errors import (ArgumentException, ArgumentNullException, ArgumentOutOfRangeException, DeviceOutOfMemoryError,
                      DeviceWaitTimeoutError, IndexOutOfRangeException, InvalidOperationException,
                      RefinementNotConvergedError)
+from .device_matrix import (AccumulatePlan, ConjugateGradientGaussPreSolver, DeviceSymmetricCSRMatrix,
+                            IterativeSolverResult, LineCrossPlan)
 from .matrix import LinearSystem, MatrixEntry, SymmetricCSRMatrix, SymmetricCSRMatrixBuilder
 from .solver import (BatchedUtduFactorization, BatchedUtduSolver, BatchedUtduSymbolic, DirectLinearSolver,
                      FillReducingOrdering, LinearSolver, Precision, ResidualCalculator, SymmetricUtduSolver,
@@ -18,5 +20,6 @@ __all__ = [
     "LinearSystem", "MatrixEntry", "SymmetricCSRMatrix", "SymmetricCSRMatrixBuilder", "DirectLinearSolver",
     "BatchedUtduFactorization", "BatchedUtduSolver", "BatchedUtduSymbolic", "FillReducingOrdering", "LinearSolver",
     "Precision", "ResidualCalculator", "SymmetricUtduSolver", "UtduNumericFactorization", "UtduSolverOptions",
-    "UtduSymbolicFactorization",
+    "UtduSymbolicFactorization", "AccumulatePlan", "ConjugateGradientGaussPreSolver", "DeviceSymmetricCSRMatrix",
+    "IterativeSolverResult", "LineCrossPlan",
 ]

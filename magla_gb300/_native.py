@@ -32,6 +32,8 @@ CUDA_ERROR = 6
 TOO_DENSE = 7
 NO_CONVERGENCE = 8
 INTERNAL = 9
+OUT_OF_RANGE = 10
+NOT_IN_PATTERN = 11
 
 PRECISION_FP64 = 0
 PRECISION_TF32 = 1
@@ -63,7 +65,7 @@ class Options(C.Structure):
         ("allow_diagonal_regularization", C.c_int), ("pivot_tolerance", C.c_double),
         ("diagonal_regularization", C.c_double), ("panel_width", C.c_int), ("precision", C.c_int),
         ("block_width", C.c_int), ("small_front_buckets", C.c_int), ("chain_merge_width", C.c_int),
-        ("inverse_block_width", C.c_int), ("device_memory_budget", C.c_int64),
+        ("inverse_block_width", C.c_int), ("device_memory_budget", C.c_int64), ("split_min_kblocks", C.c_int),
     ]
 
 
@@ -77,7 +79,8 @@ class FactorStats(C.Structure):
 
 class AutotuneReport(C.Structure):
     _fields_ = [("candidates", C.c_int), ("default_ms", C.c_double), ("best_ms", C.c_double),
-                ("small_front_buckets", C.c_int), ("block_width", C.c_int)]
+                ("small_front_buckets", C.c_int), ("block_width", C.c_int), ("chain_merge_width", C.c_int),
+                ("split_min_kblocks", C.c_int)]
 
 
 class RefineOptions(C.Structure):
@@ -95,6 +98,16 @@ class PhaseTimes(C.Structure):
                 ("launches", C.c_int), ("schur_tensor_flops", C.c_double), ("schur_tensor_ms", C.c_double),
                 ("schur_tensor_launches", C.c_int), ("solve_kind_ms", C.c_double * 14), ("solve_total_ms", C.c_double),
                 ("solve_launches", C.c_int)]
+
+class CgOptions(C.Structure):
+    _fields_ = [("relative_tolerance", C.c_double), ("max_iterations", C.c_int), ("use_preconditioner", C.c_int),
+                ("use_initial_guess", C.c_int), ("pivot_tolerance", C.c_double)]
+
+
+class CgResult(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("converged", C.c_int), ("residual_norm", C.c_double),
+                ("relative_residual", C.c_double), ("ms", C.c_double)]
+
 
 # launch kinds of PhaseTimes.solve_kind_ms
 SOLVE_KINDS = ("fwd_gather", "fwd_solo", "fwd_level", "bwd_gather", "bwd_cols", "bwd_solo", "bwd_level", "fwd_tail",
@@ -160,6 +173,24 @@ GPU_SYMBOLS = {
                                          C.c_void_p, C.c_void_p, c_int_p]),
     "uchol_set_wait_limits": (C.c_int, [C.c_double, C.c_double]),
     "uchol_check_solve_wait": (C.c_int, [C.c_void_p, C.c_double]),
+    "uchol_dmatrix_create": (C.c_int, [C.c_int, C.c_int, c_int_p, c_int_p, C.c_void_p, C.c_void_p, c_void_pp]),
+    "uchol_dmatrix_destroy": (C.c_int, [C.c_void_p]),
+    "uchol_dmatrix_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "uchol_dmatrix_values": (C.c_int, [C.c_void_p, c_void_pp]),
+    "uchol_dmatrix_set_values": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
+    "uchol_dmatrix_get_values": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
+    "uchol_dmatrix_clear_values": (C.c_int, [C.c_void_p]),
+    "uchol_accumulate_plan_create": (C.c_int, [C.c_void_p, C.c_int, c_int_p, c_int_p, c_void_pp]),
+    "uchol_accumulate": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
+    "uchol_line_cross_plan_create": (C.c_int, [C.c_void_p, C.c_int, c_int_p, c_void_pp]),
+    "uchol_line_cross": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int,
+                                   C.c_int]),
+    "uchol_values_plan_destroy": (C.c_int, [C.c_void_p]),
+    "uchol_dmatrix_multiply": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_int]),
+    "uchol_default_cg_options": (None, [C.POINTER(CgOptions)]),
+    "uchol_jacobi_pcg": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_int,
+                                   C.POINTER(CgOptions), C.POINTER(CgResult)]),
+    "uchol_refactorize_dmatrix": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(FactorStats)]),
     "uchol_kernel_launches": (C.c_int64, []),
     "uchol_set_phase_timing": (None, [C.c_int]),
     "uchol_last_error": (C.c_char_p, []),

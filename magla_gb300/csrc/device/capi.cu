@@ -284,6 +284,9 @@ struct StreamTimer {
     }
 };
 
+// K blocks of a tensor-core tile below which a launch is never split in K.
+int split_min_kb(const uchol_options& o) { return o.split_min_kblocks == 0 ? kTcMinSplitKb : o.split_min_kblocks; }
+
 PlanConfig config_for(const uchol_options& o) {
     PlanConfig c;
     c.small_mask = o.small_front_buckets ? o.small_front_buckets : 0x7;
@@ -388,7 +391,7 @@ void run_factor_launches(uchol_factor_s* F, cudaStream_t st) {
                 int nkb = (P.tc_jobs[L.begin].kn + kbe - 1) / kbe;
                 for (int j = L.begin + 1; j < L.begin + L.count; ++j)
                     if (P.tc_jobs[j].kn != P.tc_jobs[L.begin].kn) nkb = 0;
-                const TcPlanned tp = tc_schedule(L.tiles, nkb, F->sms);
+                const TcPlanned tp = tc_schedule(L.tiles, nkb, F->sms, split_min_kb(F->opts));
                 const TcSched S{L.tiles, tp.dp_tiles, tp.sk_nkb, F->tc_ws.as<float>(), F->tc_counters.as<int>()};
                 launch_tc_gemm(bf16, D.tc_jobs.as<TcJob>() + L.begin, L.count, S, tp.grid, sn, (float*)panel,
                                (float*)contrib, F->maps.as<CUtensorMap>(), &stats->status, st);
@@ -1283,6 +1286,7 @@ void uchol_default_options(uchol_options* o) {
     o->chain_merge_width = 0;
     o->inverse_block_width = 0;
     o->device_memory_budget = 0;
+    o->split_min_kblocks = 0;
 }
 
 int uchol_symbolic_create(const uchol_symbolic_desc* d, uchol_symbolic* out) {
@@ -1473,11 +1477,13 @@ int uchol_autotune(uchol_symbolic s, int n, int nnz, const double* values, const
         int candidates = 0;
         // refactorisation time of one configuration: a factor of its own, a first factorisation
         // (graph capture), then the best of two replays; +inf when the configuration fails
-        auto timed = [&](int mask, int bw) -> double {
+        auto timed = [&](int mask, int bw, int merge, int split) -> double {
             ++candidates;
             uchol_options o = o0;
             o.small_front_buckets = mask;
             o.block_width = bw;
+            o.chain_merge_width = merge;
+            o.split_min_kblocks = split;
             try {
                 std::unique_ptr<uchol_factor_s> F(create_factor(s, n, nnz, &o));
                 factorize_impl(F.get(), dv.as<double>(), true);
@@ -1495,28 +1501,41 @@ int uchol_autotune(uchol_symbolic s, int n, int nnz, const double* values, const
         };
         int mask = o0.small_front_buckets ? o0.small_front_buckets : 0x7;
         int bw = mixed ? (o0.block_width > 0 ? o0.block_width : kDiagMax) : 0;
-        const double t_default = timed(mask, bw);
+        int merge = o0.chain_merge_width, split = o0.split_min_kblocks;
+        const double t_default = timed(mask, bw, merge, split);
         double t_best = t_default;
-        for (int b = kSmallBuckets - 1; b >= 0; --b) {
-            const int m2 = mask ^ (1 << b);
-            const double t = timed(m2, bw);
+        auto keep = [&](double t) {
             if (t < t_best) {
                 t_best = t;
-                mask = m2;
+                return true;
             }
+            return false;
+        };
+        for (int b = kSmallBuckets - 1; b >= 0; --b) {
+            const int m2 = mask ^ (1 << b);
+            if (keep(timed(m2, bw, merge, split))) mask = m2;
         }
         if (mixed) {
             const int bw2 = bw == kDiagMax ? 64 : kDiagMax;
-            const double t = timed(mask, bw2);
-            if (t < t_best) {
-                t_best = t;
-                bw = bw2;
-            }
+            if (keep(timed(mask, bw2, merge, split))) bw = bw2;
         }
+        // device fronts from supernode chains: narrower, wider, or one front per supernode
+        for (int m2 : {512, 2048, -1}) {
+            if (m2 == merge) continue;
+            if (keep(timed(mask, bw, m2, split))) merge = m2;
+        }
+        // stream-K threshold of the tensor-core updates
+        if (mixed)
+            for (int s2 : {4, 16, -1}) {
+                if (s2 == split) continue;
+                if (keep(timed(mask, bw, merge, s2))) split = s2;
+            }
         *best = o0;
         best->small_front_buckets = mask;
         best->block_width = bw;
-        if (report) *report = {candidates, t_default, t_best, mask, bw};
+        best->chain_merge_width = merge;
+        best->split_min_kblocks = split;
+        if (report) *report = {candidates, t_default, t_best, mask, bw, merge, split};
     });
 }
 
@@ -1660,3 +1679,4 @@ int uchol_residual_norms(uchol_factor f, int n, int nrhs, const double* b, int l
 }  // extern "C"
 
 #include "kernel_checks.cuh"
+#include "device_matrix.cuh"

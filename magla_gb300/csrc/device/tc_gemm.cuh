@@ -609,14 +609,15 @@ struct TcPlanned {
     long long dp_tiles;
     int sk_nkb;
 };
-inline TcPlanned tc_schedule(long long tiles, int nkb, int sms) {
+// min_kb: K blocks of a tile below which it is never split (kTcMinSplitKb by default, < 0: never).
+inline TcPlanned tc_schedule(long long tiles, int nkb, int sms, int min_kb = kTcMinSplitKb) {
     TcPlanned p{(unsigned)std::max<long long>(1, std::min<long long>(tiles, sms)), tiles, 0};
-    if (nkb < kTcMinSplitKb || tiles <= 0 || tiles >= sms) return p;
+    if (min_kb < 0 || nkb < std::max(1, min_kb) || tiles <= 0 || tiles >= sms) return p;
     const long long W = tiles * nkb;
-    const long long G = std::max<long long>(1, std::min<long long>({(long long)sms, W / kTcMinSplitKb,
+    const long long G = std::max<long long>(1, std::min<long long>({(long long)sms, W / std::max(1, min_kb),
                                                                      tiles * kTcMaxParts}));
     const double t_whole = nkb;   // one wave of whole tiles
-    const double t_split = (double)((W + G - 1) / G) + kTcMinSplitKb;
+    const double t_split = (double)((W + G - 1) / G) + std::max(1, min_kb);
     if (t_split < 0.9 * t_whole) {
         p.grid = (unsigned)G;
         p.dp_tiles = 0;

@@ -59,4 +59,10 @@ def raise_for_status(status: int, message) -> None:
         raise RefinementNotConvergedError(message)
     if status == _native.TOO_DENSE:
         raise InvalidOperationException(message)
+    if status == _native.OUT_OF_RANGE:
+        err = ArgumentOutOfRangeException("")
+        err.args = (message,)
+        raise err
+    if status == _native.NOT_IN_PATTERN:
+        raise InvalidOperationException(message)
     raise InvalidOperationException(f"native call failed with status {status}: {message}")

@@ -23,6 +23,8 @@ from __future__ import annotations
 import copy
 import ctypes as C
 import enum
+import hashlib
+import json
 import os
 
 import numpy as np
@@ -63,6 +65,7 @@ class UtduSolverOptions:
         # reduced precision breaks down (a pivot regularised or not finite): factorise again in the
         # next higher precision, BF16 -> TF32 -> FP64
         self.PrecisionFallback = True
+        self.SplitMinKBlocks = 0     # stream-K threshold of the tensor-core updates (0 = 8, < 0 = never split)
         self.RefinementTolerance = 1e-12
         self.RefinementMaxIterations = 50
         for k, v in kw.items():
@@ -89,6 +92,7 @@ class UtduSolverOptions:
         o.chain_merge_width = int(self.ChainMergeWidth)
         o.inverse_block_width = int(self.InverseBlockWidth)
         o.device_memory_budget = int(self.DeviceMemoryBudget)
+        o.split_min_kblocks = int(self.SplitMinKBlocks)
         return o
 
 
@@ -435,6 +439,15 @@ class UtduNumericFactorization:
         raise_for_status(st, lib.uchol_last_error())
         self._diag = None
 
+    def RefactorizeFrom(self, dmatrix) -> None:
+        """Refactorise from the values of a DeviceSymmetricCSRMatrix (same structure): the values
+        stay on the device, and the factorisation waits for the refresh work queued on the
+        matrix's stream."""
+        lib = _native.gpu()
+        st = lib.uchol_refactorize_dmatrix(self._h, dmatrix.handle, C.byref(self._stats))
+        raise_for_status(st, lib.uchol_last_error())
+        self._diag = None
+
     def SolveRefinedDevice(self, d_b: int, d_x: int, nrhs: int = 1, tolerance: float = 1e-10,
                            max_iterations: int = 100, method: int = 0):
         """Refined solve on device buffers (column-major n x nrhs, pointers as integers)."""
@@ -567,15 +580,44 @@ class SymmetricUtduSolver(DirectLinearSolver):
     def SolveCore(self, matrix, right_hand_side):
         return self.Factorize(matrix).Solve(right_hand_side)
 
-    def Autotune(self, matrix: SymmetricCSRMatrix, symbolic: UtduSymbolicFactorization | None = None):
-        """Picks, per front-size bucket, the kernel that factorises the fronts and (mixed
-        precisions) the outer-block width, by timing refactorisations of this matrix.
+    # options the autotuner chooses (attribute of UtduSolverOptions -> field of uchol_options)
+    _TUNED = (("SmallFrontBuckets", "small_front_buckets"), ("BlockWidth", "block_width"),
+              ("ChainMergeWidth", "chain_merge_width"), ("SplitMinKBlocks", "split_min_kblocks"))
 
-        Returns (options, report): a copy of this solver's options with ``SmallFrontBuckets``
-        and ``BlockWidth`` set to the fastest configuration found, and a dict with the number of
-        candidates, the default and best refactorisation times (ms) and the choices."""
+    @staticmethod
+    def _tuning_key(matrix: SymmetricCSRMatrix, options: UtduSolverOptions) -> str:
+        """The pattern and the options that the tuned choices depend on."""
+        h = hashlib.sha256()
+        h.update(np.asarray([matrix.Size, matrix.NonZeroCount, int(options.Precision), int(options.Ordering),
+                             int(options.SupernodeAmalgamationLimit)], np.int64).tobytes())
+        h.update(np.ascontiguousarray(matrix.RowPointers, np.int32).tobytes())
+        h.update(np.ascontiguousarray(matrix.ColumnIndices, np.int32).tobytes())
+        return h.hexdigest()
+
+    def Autotune(self, matrix: SymmetricCSRMatrix, symbolic: UtduSymbolicFactorization | None = None,
+                 table: str | os.PathLike | None = None):
+        """Picks, per front-size bucket, the kernel that factorises the fronts, and the outer-block
+        width, the chain-merge width and the stream-K threshold, by timing refactorisations of this
+        matrix (uchol_autotune).
+
+        With ``table`` (a JSON file), a pattern tuned before with the same precision and ordering
+        takes its stored choices without timing anything; a new one is timed and added.
+
+        Returns (options, report): a copy of this solver's options with the chosen values, and a
+        dict with the number of candidates, the default and best refactorisation times (ms, none
+        for a stored entry), the choices and whether they came from the table."""
         if matrix is None:
             raise ArgumentNullException("matrix")
+        key = self._tuning_key(matrix, self.Options)
+        entries = {}
+        if table is not None and os.path.exists(table):
+            with open(table) as fh:
+                entries = json.load(fh)
+        tuned = copy.copy(self.Options)
+        if key in entries:
+            for attr, field in self._TUNED:
+                setattr(tuned, attr, int(entries[key][field]))
+            return tuned, dict(entries[key], candidates=0, default_ms=None, best_ms=None, from_table=True)
         if symbolic is None:
             symbolic = self.Analyze(matrix)
         else:
@@ -588,11 +630,17 @@ class SymmetricUtduSolver(DirectLinearSolver):
         st = lib.uchol_autotune(symbolic.device_handle(), matrix.Size, matrix.NonZeroCount,
                                 _native.ptr(vals, C.c_double), C.byref(base), C.byref(best), C.byref(rep))
         raise_for_status(st, lib.uchol_last_error())
-        tuned = copy.copy(self.Options)
-        tuned.SmallFrontBuckets = int(best.small_front_buckets)
-        tuned.BlockWidth = int(best.block_width)
-        report = dict(candidates=rep.candidates, default_ms=rep.default_ms, best_ms=rep.best_ms,
-                      small_front_buckets=rep.small_front_buckets, block_width=rep.block_width)
+        for attr, field in self._TUNED:
+            setattr(tuned, attr, int(getattr(best, field)))
+        choices = {field: int(getattr(best, field)) for _, field in self._TUNED}
+        report = dict(choices, candidates=rep.candidates, default_ms=rep.default_ms, best_ms=rep.best_ms,
+                      from_table=False)
+        if table is not None:
+            entries[key] = choices
+            tmp = f"{table}.tmp"
+            with open(tmp, "w") as fh:
+                json.dump(entries, fh, indent=1, sort_keys=True)
+            os.replace(tmp, table)
         return tuned, report
 
 

@@ -1,7 +1,11 @@
 """ORACLE — test infrastructure only (tests, smoke check, CPU baseline).
 
 Python wrapper of ``oracle_numeric.cpp``, the CPU restatement of the
-reference's numeric phase (CAESolvers/UCHOL/UtduNumericFactorization.cs).
+reference's numeric phase (CAESolvers/UCHOL/UtduNumericFactorization.cs),
+and of ``oracle_values.cpp``, the restatement of the values-refresh
+operations of CAESolvers/SymmetricCSRMatrix.cs (AccumulateAt, LineCross)
+and of the Jacobi-preconditioned CG of
+CAESolvers/CGGP/ConjugateGradientGaussPreSolver.cs.
 It consumes the symbolic arrays of a ``UtduSymbolicFactorization`` exactly
 as the reference's numeric phase consumes its symbolic object.  The product
 (``magla_gb300``) never imports this package.
@@ -47,6 +51,13 @@ def lib():
             L.oracle_residual_norm.argtypes = [C.c_int, _ip, _ip, _dp, _dp, _dp]
             L.oracle_multiply.argtypes = [C.c_int, _ip, _ip, _dp, _dp, _dp]
             L.oracle_multiply.restype = None
+            L.oracle_accumulate.restype = C.c_int
+            L.oracle_accumulate.argtypes = [C.c_int, _ip, _ip, _ip, _dp, C.c_int, _ip, _ip, _dp, _ip]
+            L.oracle_line_cross.restype = C.c_int
+            L.oracle_line_cross.argtypes = [C.c_int, _ip, _ip, _ip, _dp, _dp, C.c_double, C.c_int]
+            L.oracle_jacobi_pcg.restype = C.c_int
+            L.oracle_jacobi_pcg.argtypes = [C.c_int, _ip, _ip, _ip, _dp, _dp, _dp, C.c_double, C.c_int, C.c_int,
+                                            C.c_double, _dp, _ip]
             _LIB = L
         return _LIB
 
@@ -157,6 +168,75 @@ def multiply(matrix, x) -> np.ndarray:
     y = np.zeros(matrix.Size)
     lib().oracle_multiply(matrix.Size, rpp, cpp, vp, xp, y.ctypes.data_as(_dp))
     return y
+
+
+class _Csr:
+    """The structure and a private copy of the values of a SymmetricCSRMatrix."""
+
+    def __init__(self, matrix):
+        self.n = matrix.Size
+        self.rp, self.rpp = _i(matrix.RowPointers)
+        self.cp, self.cpp = _i(matrix.ColumnIndices)
+        self.dg, self.dgp = _i(matrix.DiagonalIndices)
+        self.val = np.array(matrix.Values, np.float64)
+        self.vp = self.val.ctypes.data_as(_dp)
+
+
+def accumulate(matrix, rows, cols, items):
+    """Values after AccumulateAt(rows[i], cols[i], items[i]) in order; raises
+    OracleError(1) for an index out of range, OracleError(2) for an absent
+    position (``column`` = the item)."""
+    m = _Csr(matrix)
+    r, rp = _i(rows)
+    c, cp = _i(cols)
+    v, vp = _d(items)
+    bad = C.c_int()
+    st = lib().oracle_accumulate(m.n, m.rpp, m.cpp, m.dgp, m.vp, len(r), rp, cp, vp, C.byref(bad))
+    if st:
+        raise OracleError(st, "index out of range" if st == 1 else "position absent from the structure", bad.value)
+    return m.val
+
+
+def line_cross(matrix, rhs, prescribed, indices):
+    """(values, rhs) after LineCross(rhs, prescribed[t], indices[t]) for t in order;
+    rhs may have several columns (one LineCross sequence per column, the values
+    taken from the first)."""
+    rhs = np.array(rhs, np.float64)
+    cols = rhs.reshape(rhs.shape[0], -1)
+    pres = np.asarray(prescribed, np.float64).reshape(len(indices), -1)
+    out_val = None
+    for j in range(cols.shape[1]):
+        m = _Csr(matrix)
+        b = np.ascontiguousarray(cols[:, j])
+        for t, k in enumerate(indices):
+            st = lib().oracle_line_cross(m.n, m.rpp, m.cpp, m.dgp, m.vp, b.ctypes.data_as(_dp),
+                                         float(pres[t, j]), int(k))
+            if st:
+                raise OracleError(st, "index out of range" if st == 1 else "diagonal absent", t)
+        cols[:, j] = b
+        if out_val is None:
+            out_val = m.val
+    if out_val is None:
+        out_val = np.array(matrix.Values, np.float64)
+    return out_val, cols.reshape(rhs.shape)
+
+
+def jacobi_pcg(matrix, b, x0=None, tolerance=1e-8, max_iterations=0, use_preconditioner=True,
+               pivot_tolerance=1e-300):
+    """(x, iterations, converged, residual norm, relative residual) of the
+    reference's Jacobi-PCG; raises OracleError(3) for a bad diagonal entry
+    (``column`` = its row) and OracleError(4) for p^T A p <= 0."""
+    m = _Csr(matrix)
+    bb, bp = _d(b)
+    x = np.zeros(m.n) if x0 is None else np.array(x0, np.float64)
+    out = np.zeros(4)
+    bad = C.c_int()
+    st = lib().oracle_jacobi_pcg(m.n, m.rpp, m.cpp, m.dgp, m.vp, bp, x.ctypes.data_as(_dp), tolerance,
+                                 max_iterations, 1 if use_preconditioner else 0, pivot_tolerance,
+                                 out.ctypes.data_as(_dp), C.byref(bad))
+    if st:
+        raise OracleError(st, "zero or invalid diagonal" if st == 3 else "p^T A p <= 0", bad.value)
+    return x, int(out[0]), bool(out[1]), float(out[2]), float(out[3])
 
 
 def dense_ldlt(a: np.ndarray):

@@ -1,7 +1,8 @@
 """Builds the oracle — test infrastructure only — into ``oracle/_build``.
 
 The oracle is a C++ restatement of the reference's CPU numeric phase
-(``oracle_numeric.cpp``).  It is compiled without floating-point
+(``oracle_numeric.cpp``) and of its values-refresh operations and
+Jacobi-preconditioned CG (``oracle_values.cpp``).  It is compiled without floating-point
 contraction (``-ffp-contract=off``) so its element arithmetic is the
 reference's mul-then-add on every host architecture.  The reference itself
 is C# and cannot be built in this environment (no .NET SDK), so there is no
@@ -13,16 +14,16 @@ import subprocess
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
-SRC = HERE / "oracle_numeric.cpp"
+SRCS = [HERE / "oracle_numeric.cpp", HERE / "oracle_values.cpp"]
 OUT_DIR = HERE / "_build"
 LIB = OUT_DIR / "liboracle.so"
 
 
 def build(verbose: bool = False) -> Path:
     OUT_DIR.mkdir(exist_ok=True)
-    if LIB.exists() and LIB.stat().st_mtime >= SRC.stat().st_mtime:
+    if LIB.exists() and all(LIB.stat().st_mtime >= s.stat().st_mtime for s in SRCS):
         return LIB
-    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math", str(SRC), "-o",
+    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math", *map(str, SRCS), "-o",
            str(LIB), "-lpthread"]
     if verbose:
         print(" ".join(cmd), flush=True)

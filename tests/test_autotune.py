@@ -53,12 +53,34 @@ def test_autotuned_batch_factorises_and_solves(gpu_lib):
     bs = BatchedUtduSolver(UtduSolverOptions(Precision=Precision.BF16, RefinementTolerance=1e-10))
     bsym = bs.Analyze(mats)
     tuned, rep = SymmetricUtduSolver(bs.Options).Autotune(bs.Union(mats), bsym.Union)
-    assert rep["candidates"] == 7                      # default, 5 buckets toggled, the other block width
+    # default, 5 buckets toggled, the other block width, 3 chain-merge widths, 3 stream-K thresholds
+    assert rep["candidates"] == 13 and not rep["from_table"]
     assert 0.0 < rep["best_ms"] <= rep["default_ms"]
     assert tuned.SmallFrontBuckets == rep["small_front_buckets"] and tuned.BlockWidth == rep["block_width"]
+    assert tuned.ChainMergeWidth == rep["chain_merge_width"] and tuned.SplitMinKBlocks == rep["split_min_kblocks"]
     assert tuned.BlockWidth in (64, 128)
+    assert tuned.ChainMergeWidth in (0, 512, 2048, -1) and tuned.SplitMinKBlocks in (0, 4, 16, -1)
     f = BatchedUtduSolver(tuned).Factorize(mats, bsym)
     bs_ = [build_vector(mm.Size, 30 + q) for q, mm in enumerate(mats)]
     xs = f.Solve(bs_)
     for mm, b, x in zip(mats, bs_, xs):
         assert relative_residual(mm, b, x) <= 1e-10
+
+
+@pytest.mark.gpu
+def test_autotune_table_is_persisted_and_reloaded(gpu_lib, tmp_path):
+    m = G.laplacian2d(48, 5, np.random.default_rng(3).uniform(0.0, 0.1, 48 * 48))
+    table = tmp_path / "tuning.json"
+    s = SymmetricUtduSolver(UtduSolverOptions(Precision=Precision.TF32))
+    tuned, rep = s.Autotune(m, table=table)
+    assert not rep["from_table"] and table.exists()
+    again, rep2 = s.Autotune(m, table=table)
+    assert rep2["from_table"] and rep2["candidates"] == 0
+    for attr in ("SmallFrontBuckets", "BlockWidth", "ChainMergeWidth", "SplitMinKBlocks"):
+        assert getattr(again, attr) == getattr(tuned, attr)
+    # a different precision is a different entry
+    _, rep3 = SymmetricUtduSolver(UtduSolverOptions(Precision=Precision.BF16)).Autotune(m, table=table)
+    assert not rep3["from_table"]
+    b = build_vector(m.Size, 4)
+    x = SymmetricUtduSolver(again).Factorize(m).SolveRefined(b, tolerance=1e-10)
+    assert relative_residual(m, b, x) <= 1e-10
