@@ -114,6 +114,10 @@ typedef struct {
                                            split in K (stream-K) only when its tiles have at least this many
                                            128-byte K blocks; 0 = 8, < 0 = never split.  uchol_autotune picks
                                            it. */
+    int extend_add_overlap;             /* mixed paths: the extend-add into the contribution columns of the
+                                           large fronts of a level runs on a second stream, beside the level's
+                                           outer blocks, and is joined before the level's contribution update;
+                                           0 = on, < 0 = off (one stream). */
 } uchol_options;
 
 /* Pivot statistics (UtduNumericFactorization.cs:57-84) and timings. */

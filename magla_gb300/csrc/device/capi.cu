@@ -170,7 +170,8 @@ struct uchol_symbolic_s {
         std::string key = std::to_string(c.pivot_block) + "/" + std::to_string(c.outer_block) + "/" +
                           std::to_string(c.small_mask) + "/" + std::to_string(c.tensor_core) + "/" +
                           std::to_string(c.solve_block) + "/" + std::to_string(c.merge_cols) + "/" +
-                          std::to_string(c.merge_fill) + "/" + std::to_string(c.inv_cols);
+                          std::to_string(c.merge_fill) + "/" + std::to_string(c.inv_cols) + "/" +
+                          std::to_string(c.side_extend_add);
         auto it = plans.find(key);
         if (it != plans.end()) {
             check_budget(budget, planned_bytes(it->second->plan, precision, nnz, full_nnz, n));
@@ -235,6 +236,8 @@ struct uchol_factor_s {
     int solve_graph_nrhs = 0, solve_graph_nodes = 0;
     cudaGraphExec_t factor_graph = nullptr;
     int factor_graph_nodes = 0;
+    cudaStream_t side_stream = nullptr;   // captured factorisation: the side-stream extend-add launches
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
     ~uchol_factor_s();
     DBuf maps;                    // tensor-map pairs of the staging regions
     DBuf tc_ws, tc_counters;      // K-split tiles of the tensor-core updates: partial tiles, arrival counts
@@ -258,6 +261,9 @@ uchol_factor_s::~uchol_factor_s() {
     if (solve_graph) cudaGraphExecDestroy(solve_graph);
     if (factor_graph) cudaGraphExecDestroy(factor_graph);
     if (capture_stream) cudaStreamDestroy(capture_stream);
+    if (side_stream) cudaStreamDestroy(side_stream);
+    if (fork_ev) cudaEventDestroy(fork_ev);
+    if (join_ev) cudaEventDestroy(join_ev);
     if (sym) symbolic_release(sym);
 }
 
@@ -293,6 +299,7 @@ PlanConfig config_for(const uchol_options& o) {
     c.pivot_block = std::min(kMaxPivotBlock, std::max(4, std::min(128, o.panel_width)));
     c.merge_cols = o.chain_merge_width == 0 ? kDefaultMergeCols : std::max(0, o.chain_merge_width);
     c.inv_cols = o.inverse_block_width == 0 ? kDefaultInvCols : std::max(0, o.inverse_block_width);
+    c.side_extend_add = o.extend_add_overlap >= 0;
     if (o.precision == UCHOL_PRECISION_FP64) {
         c.tensor_core = false;
         c.outer_block = c.pivot_block;
@@ -324,7 +331,25 @@ void run_factor_launches(uchol_factor_s* F, cudaStream_t st) {
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev;
     std::vector<int> ev_kind;
     const size_t small_smem = (size_t)P.max_small_m * P.max_small_m * sizeof(double);
+    // side-stream launches fork from the main stream and are joined before the launch that
+    // needs them (plan.hpp, Launch::stream); under per-launch timing everything runs in order
+    const bool overlap = !timing && F->side_stream;
+    bool side_busy = false;
+    auto join_side = [&]() {
+        CK(cudaEventRecord(F->join_ev, F->side_stream));
+        CK(cudaStreamWaitEvent(st, F->join_ev, 0));
+        side_busy = false;
+    };
     for (const Launch& L : P.launches) {
+        cudaStream_t ls = st;
+        if (overlap && L.stream == 2 && side_busy) join_side();
+        if (overlap && L.stream == 1) {
+            if (side_busy) join_side();
+            CK(cudaEventRecord(F->fork_ev, st));
+            CK(cudaStreamWaitEvent(F->side_stream, F->fork_ev, 0));
+            ls = F->side_stream;
+            side_busy = true;
+        }
         if (timing) {
             cudaEvent_t a, b;
             CK(cudaEventCreate(&a));
@@ -334,11 +359,18 @@ void run_factor_launches(uchol_factor_s* F, cudaStream_t st) {
             ev_kind.push_back((int)L.kind);
         }
         switch (L.kind) {
-            case Launch::ExtendAdd:
-                k_extend_add<T><<<(L.count + 7) / 8, 256, 0, st>>>(D.ea_items.as<EaItem>() + L.begin, L.count,
-                                                                   D.ea_entries.as<EaEntry>(), sn, D.rel.as<int>(),
-                                                                   panel, contrib);
+            case Launch::ExtendAdd: {
+                const int grid = (L.count + 7) / 8;
+                if (ls == st)
+                    k_extend_add<T><<<grid, 256, 0, ls>>>(D.ea_items.as<EaItem>() + L.begin, L.count,
+                                                          D.ea_entries.as<EaEntry>(), sn, D.rel.as<int>(), panel,
+                                                          contrib);
+                else
+                    k_extend_add<T, true><<<grid, 256, 0, ls>>>(D.ea_items.as<EaItem>() + L.begin, L.count,
+                                                                D.ea_entries.as<EaEntry>(), sn, D.rel.as<int>(), panel,
+                                                                contrib);
                 break;
+            }
             case Launch::SmallFronts:
                 k_small_fronts<T><<<L.count, 256, small_smem, st>>>(D.small.as<int>() + L.begin, sn, panel, contrib,
                                                                     diag, ctl, stats);
@@ -402,6 +434,7 @@ void run_factor_launches(uchol_factor_s* F, cudaStream_t st) {
         ++launches;
         counted();
     }
+    if (side_busy) join_side();
     CK(cudaGetLastError());
     F->phases.launches = launches;
     F->phases.schur_tensor_flops = P.tc_flops;
@@ -569,6 +602,34 @@ void enqueue_factorization(uchol_factor_s* F, cudaStream_t st) {
     }
 }
 
+// Kernel nodes of a captured factorisation: the side-stream extend-add at the lowest
+// priority, every other kernel at the highest, so that CTAs of the latency-bound chain
+// (diagonal blocks, panel solves, own-column updates) are scheduled before pending
+// extend-add CTAs.
+cudaError_t prioritise_main_stream(cudaGraph_t g) {
+    int least = 0, greatest = 0;
+    cudaError_t e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
+    if (e != cudaSuccess) return e;
+    size_t count = 0;
+    if ((e = cudaGraphGetNodes(g, nullptr, &count)) != cudaSuccess) return e;
+    std::vector<cudaGraphNode_t> nodes(count);
+    if ((e = cudaGraphGetNodes(g, nodes.data(), &count)) != cudaSuccess) return e;
+    const void* side_f = reinterpret_cast<const void*>(&k_extend_add<float, true>);
+    const void* side_d = reinterpret_cast<const void*>(&k_extend_add<double, true>);
+    for (cudaGraphNode_t nd : nodes) {
+        cudaGraphNodeType type;
+        if ((e = cudaGraphNodeGetType(nd, &type)) != cudaSuccess) return e;
+        if (type != cudaGraphNodeTypeKernel) continue;
+        cudaKernelNodeParams kp;
+        if ((e = cudaGraphKernelNodeGetParams(nd, &kp)) != cudaSuccess) return e;
+        cudaLaunchAttributeValue v;
+        memset(&v, 0, sizeof(v));
+        v.priority = (kp.func == side_f || kp.func == side_d) ? least : greatest;
+        if ((e = cudaGraphKernelNodeSetAttribute(nd, cudaLaunchAttributePriority, &v)) != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
 void factorize_impl(uchol_factor_s* F, const double* values, bool on_device) {
     uchol_symbolic_s* S = F->sym;
     cudaStream_t st = S->stream;
@@ -592,7 +653,16 @@ void factorize_impl(uchol_factor_s* F, const double* values, bool on_device) {
         CK(cudaStreamEndCapture(F->capture_stream, &g));
         F->factor_graph_nodes = (int)(g_launches.load() - before);
         g_launches -= F->factor_graph_nodes;   // counted when the graph runs
-        cudaError_t e = cudaGraphInstantiate(&F->factor_graph, g, 0);
+        unsigned long long flags = 0;
+        if (F->side_stream) {
+            cudaError_t pe = prioritise_main_stream(g);
+            if (pe != cudaSuccess) {
+                cudaGraphDestroy(g);
+                CK(pe);
+            }
+            flags = cudaGraphInstantiateFlagUseNodePriority;
+        }
+        cudaError_t e = cudaGraphInstantiateWithFlags(&F->factor_graph, g, flags);
         cudaGraphDestroy(g);
         CK(e);
         CK(cudaGraphUpload(F->factor_graph, st));
@@ -670,6 +740,13 @@ uchol_factor_s* create_factor(uchol_symbolic_s* S, int n, int nnz, const uchol_o
     F->panel.alloc((size_t)P.factor_elems * F->elem, "factor panels");
     F->contrib.alloc((size_t)P.contrib_elems * F->elem, "contribution blocks");
     CK(cudaDeviceGetAttribute(&F->sms, cudaDevAttrMultiProcessorCount, S->device));
+    bool side = false;
+    for (const Launch& L : P.launches) side |= L.stream == 1;
+    if (side) {
+        CK(cudaStreamCreateWithFlags(&F->side_stream, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&F->fork_ev, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&F->join_ev, cudaEventDisableTiming));
+    }
     if (cfg.tensor_core && P.stage_elems > 0) {
         const bool bf16 = F->precision == UCHOL_PRECISION_BF16;
         const size_t op = bf16 ? 2 : 4;
@@ -1287,6 +1364,7 @@ void uchol_default_options(uchol_options* o) {
     o->inverse_block_width = 0;
     o->device_memory_budget = 0;
     o->split_min_kblocks = 0;
+    o->extend_add_overlap = 0;
 }
 
 int uchol_symbolic_create(const uchol_symbolic_desc* d, uchol_symbolic* out) {

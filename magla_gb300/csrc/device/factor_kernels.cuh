@@ -91,57 +91,60 @@ __global__ void k_assemble(const double* __restrict__ values, const long long* _
 // block is first cleared from its diagonal down (the reference zeroes the
 // whole front, :441-447; only the lower triangle is ever read), so the
 // clearing costs no pass of its own and the adds find the lines in L2.
-template <class T>
+// Side = true: the instance launched on the side stream (its graph nodes run at
+// the lowest priority, so that the main stream's CTAs are scheduled first).
+template <class T, bool Side = false>
 __global__ void k_extend_add(const EaItem* __restrict__ items, int count, const EaEntry* __restrict__ entries,
                              const SnDev* __restrict__ sn, const int* __restrict__ rel, T* __restrict__ panel,
                              T* __restrict__ contrib) {
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
-    if (warp >= count) return;
-    const EaItem it = items[warp];
-    const SnDev P = sn[it.parent];
-    T* dst;
-    int shift;
-    if (it.pcol < P.w) {
-        dst = panel + P.panel_off + (long long)it.pcol * P.ldp;
-        shift = 0;
-    } else {
-        const int c = it.pcol - P.w, t = P.m - P.w;
-        dst = contrib + P.contrib_off + (long long)c * P.ldc;
-        shift = P.w;
-        // rows [c, t): 16-byte stores between a scalar head and tail (the column starts on a
-        // 16-byte boundary: contribution offsets are multiples of 64 elements, ldc of 8)
-        constexpr int V = 16 / (int)sizeof(T);
-        const int head = min(t, (c + V - 1) / V * V), body = max(head, t / V * V);
-        for (int r = c + lane; r < head; r += 32) dst[r] = T(0);
-        for (int v = head / V + lane; v < body / V; v += 32) reinterpret_cast<uint4*>(dst)[v] = make_uint4(0u, 0u, 0u, 0u);
-        for (int r = body + lane; r < t; r += 32) dst[r] = T(0);
-        __syncwarp();
-    }
-    for (int e = it.begin; e < it.end; ++e) {
-        const EaEntry en = entries[e];
-        const SnDev C = sn[en.child];
-        const int t = C.m - C.w;
-        const int* r = rel + C.rel_off;
-        const T* src = contrib + C.contrib_off + (long long)en.a * C.ldc;
-        // rows of one child column are distinct, so loads of a batch are issued before its stores
-        constexpr int D = 8;   // loads of a batch in flight per lane
-        for (int b0 = en.a + lane; b0 < t; b0 += 32 * D) {
-            int idx[D];
-            T sv[D], dv[D];
-#pragma unroll
-            for (int u = 0; u < D; ++u) {
-                const int b = b0 + 32 * u;
-                idx[u] = b < t ? r[b] - shift : -1;
-                sv[u] = b < t ? src[b] : T(0);
-            }
-#pragma unroll
-            for (int u = 0; u < D; ++u) dv[u] = idx[u] >= 0 ? dst[idx[u]] : T(0);
-#pragma unroll
-            for (int u = 0; u < D; ++u)
-                if (idx[u] >= 0) dst[idx[u]] = dv[u] + sv[u];
+    const int warps = gridDim.x * (blockDim.x >> 5);
+    for (int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; warp < count; warp += warps) {
+        const EaItem it = items[warp];
+        const SnDev P = sn[it.parent];
+        T* dst;
+        int shift;
+        if (it.pcol < P.w) {
+            dst = panel + P.panel_off + (long long)it.pcol * P.ldp;
+            shift = 0;
+        } else {
+            const int c = it.pcol - P.w, t = P.m - P.w;
+            dst = contrib + P.contrib_off + (long long)c * P.ldc;
+            shift = P.w;
+            // rows [c, t): 16-byte stores between a scalar head and tail (the column starts on a
+            // 16-byte boundary: contribution offsets are multiples of 64 elements, ldc of 8)
+            constexpr int V = 16 / (int)sizeof(T);
+            const int head = min(t, (c + V - 1) / V * V), body = max(head, t / V * V);
+            for (int r = c + lane; r < head; r += 32) dst[r] = T(0);
+            for (int v = head / V + lane; v < body / V; v += 32) reinterpret_cast<uint4*>(dst)[v] = make_uint4(0u, 0u, 0u, 0u);
+            for (int r = body + lane; r < t; r += 32) dst[r] = T(0);
+            __syncwarp();
         }
-        __syncwarp();
+        for (int e = it.begin; e < it.end; ++e) {
+            const EaEntry en = entries[e];
+            const SnDev C = sn[en.child];
+            const int t = C.m - C.w;
+            const int* r = rel + C.rel_off;
+            const T* src = contrib + C.contrib_off + (long long)en.a * C.ldc;
+            // rows of one child column are distinct, so loads of a batch are issued before its stores
+            constexpr int D = 8;   // loads of a batch in flight per lane
+            for (int b0 = en.a + lane; b0 < t; b0 += 32 * D) {
+                int idx[D];
+                T sv[D], dv[D];
+#pragma unroll
+                for (int u = 0; u < D; ++u) {
+                    const int b = b0 + 32 * u;
+                    idx[u] = b < t ? r[b] - shift : -1;
+                    sv[u] = b < t ? src[b] : T(0);
+                }
+#pragma unroll
+                for (int u = 0; u < D; ++u) dv[u] = idx[u] >= 0 ? dst[idx[u]] : T(0);
+#pragma unroll
+                for (int u = 0; u < D; ++u)
+                    if (idx[u] >= 0) dst[idx[u]] = dv[u] + sv[u];
+            }
+            __syncwarp();
+        }
     }
 }
 

@@ -241,7 +241,13 @@ Plan build_from_fronts(int n, int count, const int* first_column, const int* par
     const int TS = cfg.tile;
     for (int L = 0; L < P.levels; ++L) {
         const auto& fronts = at_level[L];
-        // extend-add: one item per receiving parent column
+        // extend-add: one item per receiving parent column.  With side_extend_add the items of
+        // the contribution columns of large fronts form a launch of their own, run on the side
+        // stream: nothing before the level's contribution update reads or writes those columns
+        // (the own-column updates, diagonal blocks and panel solves stay within the panel).
+        const bool side = cfg.tensor_core && cfg.side_extend_add;
+        std::vector<EaItem> side_items;
+        std::vector<EaEntry> side_entries;
         int ib = (int)P.ea_items.size();
         for (int s : fronts) {
             struct Rec { int pcol, order, child, a; };
@@ -266,14 +272,32 @@ Plan build_from_fronts(int n, int count, const int* first_column, const int* par
                 it.end = (int)P.ea_entries.size();
                 P.ea_items.push_back(it);
             }
+            const bool to_side = side && !small_front(cfg, pd.m);
+            std::vector<EaItem>& items = to_side ? side_items : P.ea_items;
+            std::vector<EaEntry>& ents = to_side ? side_entries : P.ea_entries;
             for (int pc = pd.w; pc < pd.m; ++pc) {
-                EaItem it{s, pc, (int)P.ea_entries.size(), 0};
-                for (; q < recs.size() && recs[q].pcol == pc; ++q) P.ea_entries.push_back({recs[q].child, recs[q].a});
-                it.end = (int)P.ea_entries.size();
-                P.ea_items.push_back(it);
+                EaItem it{s, pc, (int)ents.size(), 0};
+                for (; q < recs.size() && recs[q].pcol == pc; ++q) ents.push_back({recs[q].child, recs[q].a});
+                it.end = (int)ents.size();
+                items.push_back(it);
             }
         }
-        if ((int)P.ea_items.size() > ib) P.launches.push_back({Launch::ExtendAdd, ib, (int)P.ea_items.size() - ib, 0});
+        const int main_items = (int)P.ea_items.size() - ib;
+        bool side_pending = false;
+        if (!side_items.empty()) {
+            const int base = (int)P.ea_entries.size(), sb0 = (int)P.ea_items.size();
+            P.ea_entries.insert(P.ea_entries.end(), side_entries.begin(), side_entries.end());
+            for (EaItem it : side_items) {
+                it.begin += base;
+                it.end += base;
+                P.ea_items.push_back(it);
+            }
+            Launch Ls{Launch::ExtendAdd, sb0, (int)side_items.size(), 0};
+            Ls.stream = 1;
+            P.launches.push_back(Ls);
+            side_pending = true;
+        }
+        if (main_items > 0) P.launches.push_back({Launch::ExtendAdd, ib, main_items, 0});
 
         // small fronts: one CTA each
         int sb = (int)P.small_fronts.size();
@@ -422,8 +446,14 @@ Plan build_from_fronts(int n, int count, const int* first_column, const int* par
                 tiles += tc_job_tiles(d.w, d.m, d.m);
                 P.tc_flops += job_flops(U, d);
             }
-            if ((int)P.tc_jobs.size() > jb) P.launches.push_back({Launch::TcUpdate, jb, (int)P.tc_jobs.size() - jb, tiles});
+            if ((int)P.tc_jobs.size() > jb) {
+                Launch Lc{Launch::TcUpdate, jb, (int)P.tc_jobs.size() - jb, tiles};
+                Lc.stream = side_pending ? 2 : 0;   // the contribution columns are complete first
+                P.launches.push_back(Lc);
+                side_pending = false;
+            }
         }
+        if (side_pending) fail("side-stream extend-add without a contribution update to join it");
     }
 
     // ---- solves ----

@@ -32,6 +32,8 @@ struct PlanConfig {
     int merge_cols = 0;       // > 0: single-child chains of supernodes grouped into device fronts of at most
                               // this many columns (see merge_chains); 0: one device front per supernode
     double merge_fill = 0.05; // largest growth of the stored entries a grouping may cost
+    bool side_extend_add = false;   // tensor-core path: the extend-add into the contribution columns of
+                                    // large fronts runs on a second stream, beside the level's outer blocks
 };
 
 // Device fronts from the supernode partition: runs of supernodes in which each
@@ -59,6 +61,8 @@ struct Launch {
     } kind;
     int begin, count;   // task range
     long long tiles;    // update launches: total tiles (= grid size)
+    int stream = 0;     // 0: main stream; 1: side stream, forked from the main stream at this point;
+                        // 2: main stream after joining the side stream
 };
 
 struct SolveLaunch {

@@ -66,6 +66,7 @@ class UtduSolverOptions:
         # next higher precision, BF16 -> TF32 -> FP64
         self.PrecisionFallback = True
         self.SplitMinKBlocks = 0     # stream-K threshold of the tensor-core updates (0 = 8, < 0 = never split)
+        self.ExtendAddOverlap = 0    # extend-add of contribution columns on a second stream (0 = on, < 0 = off)
         self.RefinementTolerance = 1e-12
         self.RefinementMaxIterations = 50
         for k, v in kw.items():
@@ -93,6 +94,7 @@ class UtduSolverOptions:
         o.inverse_block_width = int(self.InverseBlockWidth)
         o.device_memory_budget = int(self.DeviceMemoryBudget)
         o.split_min_kblocks = int(self.SplitMinKBlocks)
+        o.extend_add_overlap = int(self.ExtendAddOverlap)
         return o
 
 
