@@ -98,7 +98,7 @@ typedef struct {
     int chain_merge_width;              /* device fronts: runs of supernodes in which each is the only child of
                                            the next are factorised as one front of at most this many columns
                                            when that adds at most 5% stored entries (exact zeros); the symbolic
-                                           partition itself is unchanged.  0 = 1024, < 0 = one front per
+                                           partition itself is unchanged.  0 = 2048, < 0 = one front per
                                            supernode. */
     int inverse_block_width;            /* solves: fronts of more than one solve block (128 columns mixed, 64
                                            FP64) and at most this many columns keep the inverse of their
@@ -221,7 +221,7 @@ typedef struct {
     double best_ms;              /* of the chosen configuration */
     int small_front_buckets;     /* chosen bucket mask */
     int block_width;             /* chosen outer-block width (mixed paths; 0 on the FP64 path) */
-    int chain_merge_width;       /* chosen chain_merge_width (0 = the default, 1024) */
+    int chain_merge_width;       /* chosen chain_merge_width (0 = the default, 2048) */
     int split_min_kblocks;       /* chosen split_min_kblocks (0 = the default, 8) */
 } uchol_autotune_report;
 int uchol_autotune(uchol_symbolic s, int n, int nnz, const double* values, const uchol_options* base,

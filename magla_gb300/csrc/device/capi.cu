@@ -1598,7 +1598,7 @@ int uchol_autotune(uchol_symbolic s, int n, int nnz, const double* values, const
             if (keep(timed(mask, bw2, merge, split))) bw = bw2;
         }
         // device fronts from supernode chains: narrower, wider, or one front per supernode
-        for (int m2 : {512, 2048, -1}) {
+        for (int m2 : {512, 1024, -1}) {
             if (m2 == merge) continue;
             if (keep(timed(mask, bw, m2, split))) merge = m2;
         }

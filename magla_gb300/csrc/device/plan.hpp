@@ -18,7 +18,7 @@ constexpr int kColRowsPlan = 2048;   // trailing rows per backward column-dot ta
 constexpr int kInvColRowsPlan = 1024;   // trailing rows per backward partial-sum task of an inverse front
 constexpr int kDefaultInvCols = 2048;   // widest front whose diagonal block is kept inverted for the solves
 constexpr int kSuperBlocks = 4;       // tensor-core path: outer blocks per super-block of the own-column updates
-constexpr int kDefaultMergeCols = 1024;   // widest device front made of a chain of supernodes (merge_chains)
+constexpr int kDefaultMergeCols = 2048;   // widest device front made of a chain of supernodes (merge_chains)
 
 struct PlanConfig {
     int pivot_block = 32;     // FP64 pivot block (the reference's PanelWidth)

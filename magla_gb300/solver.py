@@ -59,7 +59,7 @@ class UtduSolverOptions:
         self.Precision = Precision.FP64
         self.BlockWidth = 0
         self.SmallFrontBuckets = 0   # bit b: fronts of 32b < m <= 32(b+1) rows go whole to one CTA (0 = 0x7)
-        self.ChainMergeWidth = 0     # widest device front grouped from a chain of supernodes (0 = 1024, < 0 = off)
+        self.ChainMergeWidth = 0     # widest device front grouped from a chain of supernodes (0 = 2048, < 0 = off)
         self.InverseBlockWidth = 0   # widest front whose diagonal block is kept inverted for the solves (0 = 2048, < 0 = off)
         self.DeviceMemoryBudget = 0  # bytes; > 0: factorisations needing more fail with OOM before allocating
         # reduced precision breaks down (a pivot regularised or not finite): factorise again in the
