@@ -118,6 +118,8 @@ typedef struct {
                                            large fronts of a level runs on a second stream, beside the level's
                                            outer blocks, and is joined before the level's contribution update;
                                            0 = on, < 0 = off (one stream). */
+    double chain_merge_fill;            /* device fronts from supernode chains: the largest relative growth
+                                           of the stored entries a grouping may cost; 0 = 0.05. */
 } uchol_options;
 
 /* Pivot statistics (UtduNumericFactorization.cs:57-84) and timings. */

@@ -66,7 +66,7 @@ class Options(C.Structure):
         ("diagonal_regularization", C.c_double), ("panel_width", C.c_int), ("precision", C.c_int),
         ("block_width", C.c_int), ("small_front_buckets", C.c_int), ("chain_merge_width", C.c_int),
         ("inverse_block_width", C.c_int), ("device_memory_budget", C.c_int64), ("split_min_kblocks", C.c_int),
-        ("extend_add_overlap", C.c_int),
+        ("extend_add_overlap", C.c_int), ("chain_merge_fill", C.c_double),
     ]
 
 

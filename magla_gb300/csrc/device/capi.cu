@@ -300,6 +300,7 @@ PlanConfig config_for(const uchol_options& o) {
     c.merge_cols = o.chain_merge_width == 0 ? kDefaultMergeCols : std::max(0, o.chain_merge_width);
     c.inv_cols = o.inverse_block_width == 0 ? kDefaultInvCols : std::max(0, o.inverse_block_width);
     c.side_extend_add = o.extend_add_overlap >= 0;
+    if (o.chain_merge_fill > 0.0) c.merge_fill = o.chain_merge_fill;
     if (o.precision == UCHOL_PRECISION_FP64) {
         c.tensor_core = false;
         c.outer_block = c.pivot_block;
@@ -710,6 +711,8 @@ void check_options(const uchol_options* o) {
     if (!(o->pivot_tolerance >= 0.0) || !(o->diagonal_regularization > 0.0))
         throw Error(UCHOL_BAD_ARG, "pivot tolerance must be >= 0 and regularization > 0");
     if (o->device_memory_budget < 0) throw Error(UCHOL_BAD_ARG, "the device memory budget must be >= 0");
+    if (!(o->chain_merge_fill >= 0.0) || o->chain_merge_fill > 10.0)
+        throw Error(UCHOL_BAD_ARG, "chain_merge_fill must be in [0, 10]");
     if (o->small_front_buckets < 0 || o->small_front_buckets >= (1 << kSmallBuckets))
         throw Error(UCHOL_BAD_ARG, "small_front_buckets has bits beyond the " + std::to_string(kSmallBuckets) +
                                        " front-size buckets");
@@ -1365,6 +1368,7 @@ void uchol_default_options(uchol_options* o) {
     o->device_memory_budget = 0;
     o->split_min_kblocks = 0;
     o->extend_add_overlap = 0;
+    o->chain_merge_fill = 0.0;
 }
 
 int uchol_symbolic_create(const uchol_symbolic_desc* d, uchol_symbolic* out) {

@@ -67,6 +67,7 @@ class UtduSolverOptions:
         self.PrecisionFallback = True
         self.SplitMinKBlocks = 0     # stream-K threshold of the tensor-core updates (0 = 8, < 0 = never split)
         self.ExtendAddOverlap = 0    # extend-add of contribution columns on a second stream (0 = on, < 0 = off)
+        self.ChainMergeFill = 0.0    # largest growth of stored entries a chain grouping may cost (0 = 0.05)
         self.RefinementTolerance = 1e-12
         self.RefinementMaxIterations = 50
         for k, v in kw.items():
@@ -95,6 +96,7 @@ class UtduSolverOptions:
         o.device_memory_budget = int(self.DeviceMemoryBudget)
         o.split_min_kblocks = int(self.SplitMinKBlocks)
         o.extend_add_overlap = int(self.ExtendAddOverlap)
+        o.chain_merge_fill = float(self.ChainMergeFill)
         return o
 
 
@@ -353,12 +355,14 @@ class UtduNumericFactorization:
             self._diag = d
         return self._diag
 
-    def Solve(self, right_hand_side) -> np.ndarray:
+    def Solve(self, right_hand_side, out: np.ndarray | None = None) -> np.ndarray:
         """x = A^-1 b (b may be a vector or an n x k block of right-hand sides).
 
         A FP64 factor is applied once, as in the reference.  A mixed-precision
         factor is refined against the FP64 matrix until the relative residual
-        of every column reaches ``RefinementTolerance``.
+        of every column reaches ``RefinementTolerance``.  ``out`` (optional): a
+        float64 array of b's shape, column-major for a block (for example in
+        page-locked memory), that receives x and is returned.
         """
         if right_hand_side is None:
             raise ArgumentNullException("rightHandSide")
@@ -367,24 +371,41 @@ class UtduNumericFactorization:
         if b.shape[0] != n:
             raise ArgumentException(f"The right-hand side length {b.shape[0]} does not match the matrix size {n}.")
         if self.Precision != Precision.FP64:
-            return self.SolveRefined(b, self._options.RefinementTolerance, self._options.RefinementMaxIterations)
-        return self._apply(b)
+            return self.SolveRefined(b, self._options.RefinementTolerance, self._options.RefinementMaxIterations,
+                                     out=out)
+        return self._apply(b, out)
 
-    def _apply(self, b):
+    @staticmethod
+    def _out_block(b, out):
+        """The column-major n x k block x is written to (a view of ``out`` when given)."""
+        if out is None:
+            return np.zeros((b.shape[0], 1 if b.ndim == 1 else b.shape[1]), order="F")
+        if out.shape != b.shape or out.dtype != np.float64:
+            raise ArgumentException(f"out must be a float64 array of shape {b.shape}", "out")
+        X = out.reshape(b.shape[0], -1, order="F")
+        if not X.flags.f_contiguous or not np.shares_memory(X, out):
+            raise ArgumentException("out must be column-major (Fortran order)", "out")
+        return X
+
+    def _apply(self, b, out=None):
         lib = _native.gpu()
         vec = b.ndim == 1
         if self.Size == 0:
-            return np.zeros(b.shape)
+            return np.zeros(b.shape) if out is None else out
         B = np.asfortranarray(b.reshape(b.shape[0], -1))
-        X = np.zeros_like(B, order="F")
+        X = self._out_block(b, out)
         k = B.shape[1]
         ld = max(1, B.shape[0])
         st = lib.uchol_solve(self._h, self.Size, k, _native.ptr(B, C.c_double), ld, _native.ptr(X, C.c_double), ld)
         raise_for_status(st, lib.uchol_last_error())
+        if out is not None:
+            return out
         return X[:, 0].copy() if vec else X
 
-    def SolveRefined(self, right_hand_side, tolerance: float = 1e-10, max_iterations: int = 50, method: int = 0):
-        """Solve with FP64-residual refinement; statistics land in ``LastRefinement``."""
+    def SolveRefined(self, right_hand_side, tolerance: float = 1e-10, max_iterations: int = 50, method: int = 0,
+                     out: np.ndarray | None = None):
+        """Solve with FP64-residual refinement; statistics land in ``LastRefinement``.  ``out`` as in
+        ``Solve``."""
         lib = _native.gpu()
         b = np.asarray(right_hand_side, dtype=np.float64)
         if b.shape[0] != self.Size:
@@ -392,9 +413,9 @@ class UtduNumericFactorization:
         vec = b.ndim == 1
         if self.Size == 0:
             self.LastRefinement = _native.RefineStats()
-            return np.zeros(b.shape)
+            return np.zeros(b.shape) if out is None else out
         B = np.asfortranarray(b.reshape(b.shape[0], -1))
-        X = np.zeros_like(B, order="F")
+        X = self._out_block(b, out)
         ro = _native.RefineOptions(float(tolerance), int(max_iterations), int(method))
         rs = _native.RefineStats()
         ld = max(1, B.shape[0])
@@ -402,6 +423,8 @@ class UtduNumericFactorization:
                                      _native.ptr(X, C.c_double), ld, C.byref(ro), C.byref(rs))
         self.LastRefinement = rs
         raise_for_status(st, lib.uchol_last_error())
+        if out is not None:
+            return out
         return X[:, 0].copy() if vec else X
 
     def DeviceResidualNorms(self, b, x) -> np.ndarray:

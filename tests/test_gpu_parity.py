@@ -352,3 +352,22 @@ def test_symbolic_handle_destroyed_before_its_factor(gpu_lib):
     f.Refactorize(m)
     assert np.array_equal(f.Solve(b), x0)
     f.__del__()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", ["FP64", "TF32"])
+def test_solve_into_caller_buffer(gpu_lib, prec):
+    """Solve(b, out=x): x receives the solution (column-major block or vector) and is returned."""
+    m = G.elasticity(5, 5, 4)[0]
+    opts = UtduSolverOptions(Precision=Precision[prec])
+    f = SymmetricUtduSolver(opts).Factorize(m)
+    B = np.asfortranarray(np.stack([build_vector(m.Size, 7), build_vector(m.Size, 8)], axis=1))
+    X = np.zeros_like(B, order="F")
+    got = f.Solve(B, out=X)
+    assert got is X
+    assert np.array_equal(X, f.Solve(B))
+    x1 = np.zeros(m.Size)
+    assert f.Solve(B[:, 0].copy(), out=x1) is x1
+    assert np.array_equal(x1, f.Solve(B[:, 0].copy()))
+    with pytest.raises(ArgumentException):
+        f.Solve(B, out=np.zeros((m.Size, 2)))   # row-major block
