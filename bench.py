@@ -66,6 +66,8 @@ def parse():
                    help="> 1: Young's modulus log-uniform in [1, contrast] per element (seeded), the "
                         "stiffness-contrast elasticity case (1e4)")
     p.add_argument("--tol", type=float, default=1e-10)
+    p.add_argument("--chain-merge-width", type=int, default=0,
+                   help="widest device front grouped from a chain of supernodes (0: the library default, 2048)")
     p.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 GPU arm")
     p.add_argument("--cpu-sample-elements", type=int, nargs=3, default=None,
                    help="mesh of the CPU baseline sample (default: 0.3 x the workload's mesh, at least 8)")
@@ -224,6 +226,7 @@ def run_ours(args):
     ordering = mg.FillReducingOrdering["ApproximateMinimumDegree" if args.ordering == "AMD" else "Natural"]
     prec = mg.Precision[args.precision]
     opts = mg.UtduSolverOptions(Ordering=ordering, Precision=prec, RefinementTolerance=args.tol,
+                                ChainMergeWidth=args.chain_merge_width,
                                 RefinementMaxIterations=200)
     solver = mg.SymmetricUtduSolver(opts)
     t_sym = time.perf_counter()
@@ -243,7 +246,8 @@ def run_ours(args):
     fp64 = None
     x64 = None
     if not args.no_fp64 and prec != mg.Precision.FP64:
-        s64 = mg.SymmetricUtduSolver(mg.UtduSolverOptions(Ordering=ordering, Precision=mg.Precision.FP64))
+        s64 = mg.SymmetricUtduSolver(mg.UtduSolverOptions(Ordering=ordering, Precision=mg.Precision.FP64,
+                                                          ChainMergeWidth=args.chain_merge_width))
         f64 = s64.FactorizeDevice(m, sym, d_sets[0].data_ptr())
         factor64_s = f64.FactorMilliseconds / 1e3
         f64.SolveDevice(d_b.data_ptr(), d_x.data_ptr(), nrhs)   # first call captures the solve graph
@@ -400,7 +404,7 @@ def gemm_traffic(args, prec):
     import magla_gb300 as mg
     f = ROOT / "profiles" / "k_tc_gemm_dram_elasticity80x80x40_tf32.txt"
     if list(args.elements) != [80, 80, 40] or prec != mg.Precision.TF32 or args.ordering != "Natural" \
-            or not f.exists():
+            or args.chain_merge_width != 0 or not f.exists():
         return None
     for line in f.read_text().splitlines():
         if line.startswith("traffic_bytes_per_launch:"):
