@@ -225,6 +225,7 @@ struct uchol_factor_s {
     DBuf linv;                          // inverses of the diagonal blocks (solves)
     DBuf linv_off;                      // inverse fronts: off-diagonal blocks of the diagonal block's inverse
     DBuf inv_partial;                   // inverse fronts: backward partial sums (solve workspace)
+    DBuf inv_diag_partial, inv_diag_cnt;   // inverse fronts: chunk partial sums of the diagonal products, counters
     DBuf minv;                          // mixed path: per outer block X^T, D, D^{-1} of each diagonal block
     DBuf solve_flags;                   // per diagonal block: forward and backward "solution published" flags
     DBuf solve_maps;                    // per front: tensor maps of its panel, boxes SB x SB, SB x SB/2, SB/2 x SB
@@ -887,7 +888,7 @@ void run_solve(uchol_factor_s* F, int nrhs, Cv* work, Cv* fv, Cv* fv2, cudaStrea
     int* status = F->solve_status.as<int>();
     CK(cudaMemsetAsync(fwd_flags, 0, sizeof(int) * ((size_t)2 * nblocks + P.progress_count), st));
     const size_t smem = level_smem_bytes<T, Cv, SB, RG>();
-    constexpr int RGD = RG == 1 ? 1 : 4;   // right-hand sides per CTA of the inverse-front diagonal kernels
+    constexpr int RGD = RG == 1 ? 1 : 8;   // right-hand sides per CTA of the inverse-front diagonal kernels
     auto level_args = [&](const SolveLaunch& L, int* flags, int grid) {
         LevelArgs la;
         la.chains = tasks + L.begin;
@@ -928,7 +929,8 @@ void run_solve(uchol_factor_s* F, int nrhs, Cv* work, Cv* fv, Cv* fv2, cudaStrea
             k_fwd_solo<T, Cv, SB><<<L.count, 256, 0, st>>>(tasks + L.begin, A, panel, linv, fv, fv2, diag, work);
         } else if (L.kind == SolveLaunch::FwdInvDiag) {
             k_fwd_inv_diag<T, Cv, SB, RGD><<<dim3(L.count, (nrhs + RGD - 1) / RGD), 256, inv_solve_smem<T, Cv, SB, RGD>(), st>>>(
-                tasks + L.begin, A, linv, F->linv_off.as<Cv>(), fv, fv2, diag, work, status);
+                tasks + L.begin, A, linv, F->linv_off.as<Cv>(), fv, fv2, diag, work, F->inv_diag_partial.as<Cv>(),
+                F->inv_diag_cnt.as<unsigned>(), status);
         } else if (L.kind == SolveLaunch::FwdInvTail) {
             k_fwd_inv_tail<T, Cv, SB, RG><<<L.count, 256, inv_tail_smem<T, Cv, SB, RG, false>(), st>>>(
                 tasks + L.begin, A, F->solve_maps.as<CUtensorMap>() + P.count, fv2, fv, status);
@@ -961,7 +963,8 @@ void run_solve(uchol_factor_s* F, int nrhs, Cv* work, Cv* fv, Cv* fv2, cudaStrea
                                                                                         F->inv_partial.as<Cv>());
         } else if (L.kind == SolveLaunch::BwdInvDiag) {
             k_bwd_inv_diag<T, Cv, SB, RGD><<<dim3(L.count, (nrhs + RGD - 1) / RGD), 256, inv_solve_smem<T, Cv, SB, RGD>(), st>>>(
-                tasks + L.begin, A, linv, F->linv_off.as<Cv>(), fv, work, status);
+                tasks + L.begin, A, linv, F->linv_off.as<Cv>(), fv, work, F->inv_diag_partial.as<Cv>(),
+                F->inv_diag_cnt.as<unsigned>(), status);
         } else if (L.kind == SolveLaunch::BwdSolo) {
             k_bwd_solo<Cv, SB><<<L.count, 256, 0, st>>>(tasks + L.begin, A, linv, fv, fv2, work);
         } else {
@@ -1011,12 +1014,12 @@ void launch_solve_graph(uchol_factor_s* F, int nrhs, Cv* work, cudaStream_t st) 
         // inverse-front kernels of both groupings
         CK(cudaFuncSetAttribute(k_fwd_inv_diag<T, Cv, SB, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)inv_solve_smem<T, Cv, SB, 1>()));
-        CK(cudaFuncSetAttribute(k_fwd_inv_diag<T, Cv, SB, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)inv_solve_smem<T, Cv, SB, 4>()));
+        CK(cudaFuncSetAttribute(k_fwd_inv_diag<T, Cv, SB, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)inv_solve_smem<T, Cv, SB, 8>()));
         CK(cudaFuncSetAttribute(k_bwd_inv_diag<T, Cv, SB, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)inv_solve_smem<T, Cv, SB, 1>()));
-        CK(cudaFuncSetAttribute(k_bwd_inv_diag<T, Cv, SB, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)inv_solve_smem<T, Cv, SB, 4>()));
+        CK(cudaFuncSetAttribute(k_bwd_inv_diag<T, Cv, SB, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)inv_solve_smem<T, Cv, SB, 8>()));
         CK(cudaFuncSetAttribute(k_fwd_inv_tail<T, Cv, SB, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)inv_tail_smem<T, Cv, SB, 1, false>()));
         CK(cudaFuncSetAttribute(k_fwd_inv_tail<T, Cv, SB, kSolveRhsGroup>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1156,6 +1159,9 @@ void ensure_workspace(uchol_factor_s* F, int nrhs) {
     F->fv2.alloc((size_t)P.fvec_elems * nrhs * cv, "solve workspace");
     F->bwd_partial.alloc((size_t)std::max(1, P.bwd_partial_slots) * 8 * nrhs * cv, "solve workspace");
     F->inv_partial.alloc((size_t)std::max(1, P.inv_partial_slots) * P.cfg.solve_block * nrhs * cv, "solve workspace");
+    F->inv_diag_partial.alloc((size_t)std::max(1, P.inv_diag_slots) * P.cfg.solve_block * nrhs * cv, "solve workspace");
+    F->inv_diag_cnt.alloc((size_t)std::max(1, P.inv_diag_slots) * nrhs * sizeof(unsigned), "solve workspace");
+    CK(cudaMemsetAsync(F->inv_diag_cnt.p, 0, F->inv_diag_cnt.bytes, S->stream));   // the last chunk resets each
     if (F->solve_graph) {
         CK(cudaGraphExecDestroy(F->solve_graph));
         F->solve_graph = nullptr;

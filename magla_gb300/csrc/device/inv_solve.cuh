@@ -138,6 +138,43 @@ struct RhsPrefetch {
     }
 };
 
+// Inverse-diagonal products split in chunks of blocks (plan.hpp, FwdInvDiag): a CTA stores
+// the partial sums v of its chunk (row `row`, right-hand sides g0 .. g0+FG-1 of the group) in
+// slot slot0 + chunk and counts itself in; the CTA that completes the row's nc chunks adds
+// the nc partial sums in chunk order into v and returns true, the others return false.  No
+// CTA waits for another.  nc = 1: v is already complete.
+template <class Cv, int SB, int FG>
+__device__ __forceinline__ bool inv_chunk_combine(Cv (&v)[FG], bool fin, int row, int g0, int ng, int rg, int nrhs,
+                                                  int slot0, int chunk, int nc, Cv* __restrict__ pbuf,
+                                                  unsigned* __restrict__ cnt) {
+    if (nc == 1) return true;
+    __shared__ int last;
+    if (fin) {
+#pragma unroll
+        for (int q = 0; q < FG; ++q)
+            if (g0 + q < ng) pbuf[((long long)(slot0 + chunk) * nrhs + rg + g0 + q) * SB + row] = v[q];
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned* c = cnt + (long long)slot0 * gridDim.y + blockIdx.y;
+        last = atomicAdd(c, 1u) == (unsigned)(nc - 1);
+        if (last) *c = 0u;   // every chunk has counted in: ready for the next launch
+    }
+    __syncthreads();
+    if (!last) return false;
+    if (fin) {
+#pragma unroll
+        for (int q = 0; q < FG; ++q) {
+            Cv s = Cv(0);
+            if (g0 + q < ng)
+                for (int k = 0; k < nc; ++k) s += __ldcg(&pbuf[((long long)(slot0 + k) * nrhs + rg + g0 + q) * SB + row]);
+            v[q] = s;
+        }
+    }
+    return true;
+}
+
 // Forward y_i = sum_{j <= i} Linv(i, j) f_j for right-hand sides [RG blockIdx.y, +RG);
 // writes y_i (front vector yv) and y_i / D (work).  Thread (row, pid) sums columns
 // [pid CPT, pid CPT + CPT) of each block.
@@ -146,6 +183,7 @@ __global__ void __launch_bounds__(256, 1) k_fwd_inv_diag(const SolveBlockTask* _
                                                          const Cv* __restrict__ linv, const Cv* __restrict__ linv_off,
                                                          const Cv* __restrict__ fv, Cv* __restrict__ yv,
                                                          const double* __restrict__ diag, Cv* __restrict__ work,
+                                                         Cv* __restrict__ pbuf, unsigned* __restrict__ cnt,
                                                          int* status) {
     using R = LevelRhs<Cv, SB, RG>;
     constexpr int TPR = R::TP, CPT = SB / TPR, RS = R::RS, FG = R::FG;
@@ -159,7 +197,7 @@ __global__ void __launch_bounds__(256, 1) k_fwd_inv_diag(const SolveBlockTask* _
     __shared__ unsigned long long bar[2];
     const SolveBlockTask tk = tasks[blockIdx.x];
     const SnDev d = A.sn[tk.s];
-    const int i = tk.k0, ob = tk.r0, blk = tk.blk;
+    const int i = tk.k0, ob = tk.r0, blk = tk.blk, j0 = tk.c0, j1 = tk.c1;
     const int rg = blockIdx.y * RG, ng = min(RG, A.nrhs - rg);
     const int tid = threadIdx.x, row = tid % SB, pid = tid / SB;
     const bool fin = RG >= TPR || pid == 0;
@@ -172,9 +210,10 @@ __global__ void __launch_bounds__(256, 1) k_fwd_inv_diag(const SolveBlockTask* _
     constexpr unsigned kTileBytes = SB * SB * sizeof(Cv);
     auto issue = [&](int jj) {
         if (tid == 0) {
+            const int st = (jj - j0) & 1;
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            bar_expect(&bar[jj & 1], kTileBytes);
-            bulk_g2s(stage(jj & 1), inv_block<Cv, SB>(linv, linv_off, blk, ob, i, jj), kTileBytes, &bar[jj & 1]);
+            bar_expect(&bar[st], kTileBytes);
+            bulk_g2s(stage(st), inv_block<Cv, SB>(linv, linv_off, blk, ob, i, jj), kTileBytes, &bar[st]);
         }
     };
     // f_j, zero past the front's columns and the group's right-hand sides
@@ -185,20 +224,21 @@ __global__ void __launch_bounds__(256, 1) k_fwd_inv_diag(const SolveBlockTask* _
             return (g < ng && col < d.w) ? fv[fo + (long long)(rg + g) * A.fv_stride + col] : Cv(0);
         });
     };
-    fetch(0);
+    fetch(j0);
     __syncthreads();   // barriers initialised
-    issue(0);
-    if (i >= 1) issue(1);
+    issue(j0);
+    if (j0 + 1 <= j1) issue(j0 + 1);
     pf.commit(fbuf(0));
-    if (i >= 1) fetch(1);
+    if (j0 + 1 <= j1) fetch(j0 + 1);
     RhsAcc<Cv, RG> acc;
     acc.zero();
     unsigned phase = 0;
-    for (int j = 0; j <= i; ++j) {
-        if (!__syncthreads_and(bar_wait(&bar[j & 1], (phase >> (j & 1)) & 1u, status))) return;
-        phase ^= 1u << (j & 1);
-        const Cv* tile = stage(j & 1);
-        const Cv* fb = fbuf(j & 1);
+    for (int j = j0; j <= j1; ++j) {
+        const int st = (j - j0) & 1;
+        if (!__syncthreads_and(bar_wait(&bar[st], (phase >> st) & 1u, status))) return;
+        phase ^= 1u << st;
+        const Cv* tile = stage(st);
+        const Cv* fb = fbuf(st);
 #pragma unroll 2
         for (int u0 = 0; u0 < CPT; u0 += 4)
 #pragma unroll
@@ -206,25 +246,36 @@ __global__ void __launch_bounds__(256, 1) k_fwd_inv_diag(const SolveBlockTask* _
                 const int c = pid * CPT + u0 + q;
                 acc.add(q, tile[row + c * SB], fb + c * RS);
             }
-        if (j + 1 <= i) pf.commit(fbuf((j + 1) & 1));
-        if (j + 2 <= i) fetch(j + 2);
+        if (j + 1 <= j1) pf.commit(fbuf(st ^ 1));
+        if (j + 2 <= j1) fetch(j + 2);
         __syncthreads();   // the stage is free again
-        if (j + 2 <= i) issue(j + 2);
+        if (j + 2 <= j1) issue(j + 2);
     }
     acc.store(part + (pid * SB + row) * RG);
     __syncthreads();
+    Cv y[FG];
+#pragma unroll
+    for (int q = 0; q < FG; ++q) {
+        const int g = g0 + q;
+        y[q] = Cv(0);
+        if (fin && g < ng) {
+            y[q] = part[row * RG + g];
+#pragma unroll
+            for (int p = 1; p < TPR; ++p) y[q] += part[(p * SB + row) * RG + g];
+        }
+    }
+    if (!inv_chunk_combine<Cv, SB, FG>(y, fin, row, g0, ng, rg, A.nrhs, tk.r1, j0 / kInvDiagChunk, tk.flags, pbuf,
+                                       cnt))
+        return;
     if (fin) {
         const int kn = min(SB, d.w - i * SB);
 #pragma unroll
         for (int q = 0; q < FG; ++q) {
             const int g = g0 + q;
             if (g >= ng || row >= kn) break;
-            Cv y = part[row * RG + g];
-#pragma unroll
-            for (int p = 1; p < TPR; ++p) y += part[(p * SB + row) * RG + g];
             const int col = i * SB + row;
-            yv[fo + (long long)(rg + g) * A.fv_stride + col] = y;
-            work[d.first_col + col + (long long)(rg + g) * A.ldw] = (Cv)((double)y / diag[d.first_col + col]);
+            yv[fo + (long long)(rg + g) * A.fv_stride + col] = y[q];
+            work[d.first_col + col + (long long)(rg + g) * A.ldw] = (Cv)((double)y[q] / diag[d.first_col + col]);
         }
     }
 }
@@ -537,6 +588,7 @@ template <class T, class Cv, int SB, int RG>
 __global__ void __launch_bounds__(256, 1) k_bwd_inv_diag(const SolveBlockTask* __restrict__ tasks, SolveArgs A,
                                                          const Cv* __restrict__ linv, const Cv* __restrict__ linv_off,
                                                          const Cv* __restrict__ fv, Cv* __restrict__ work,
+                                                         Cv* __restrict__ pbuf, unsigned* __restrict__ cnt,
                                                          int* status) {
     using R = LevelRhs<Cv, SB, RG>;
     constexpr int TPC = R::TP, RPT = SB / TPC, RS = R::RS, FG = R::FG;
@@ -550,7 +602,7 @@ __global__ void __launch_bounds__(256, 1) k_bwd_inv_diag(const SolveBlockTask* _
     __shared__ unsigned long long bar[2];
     const SolveBlockTask tk = tasks[blockIdx.x];
     const SnDev d = A.sn[tk.s];
-    const int j = tk.k0, nb = tk.kn, ob = tk.r0, blk = tk.blk;
+    const int j = tk.k0, ob = tk.r0, blk = tk.blk, i0 = tk.c0, i1 = tk.c1;
     const int rg = blockIdx.y * RG, ng = min(RG, A.nrhs - rg);
     const int tid = threadIdx.x, ccol = tid % SB, cpart = tid / SB;
     const bool fin = RG >= TPC || cpart == 0;
@@ -564,7 +616,7 @@ __global__ void __launch_bounds__(256, 1) k_bwd_inv_diag(const SolveBlockTask* _
     auto issue = [&](int ii) {
         if (tid == 0) {
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            const int st = (ii - j) & 1;
+            const int st = (ii - i0) & 1;
             bar_expect(&bar[st], kTileBytes);
             bulk_g2s(stage(st), inv_block<Cv, SB>(linv, linv_off, blk, ob, ii, j), kTileBytes, &bar[st]);
         }
@@ -576,17 +628,17 @@ __global__ void __launch_bounds__(256, 1) k_bwd_inv_diag(const SolveBlockTask* _
             return (g < ng && col < d.w) ? fv[fo + (long long)(rg + g) * A.fv_stride + col] : Cv(0);
         });
     };
-    fetch(j);
+    fetch(i0);
     __syncthreads();   // barriers initialised
-    issue(j);
-    if (j + 1 < nb) issue(j + 1);
+    issue(i0);
+    if (i0 + 1 <= i1) issue(i0 + 1);
     pf.commit(gbuf(0));
-    if (j + 1 < nb) fetch(j + 1);
+    if (i0 + 1 <= i1) fetch(i0 + 1);
     RhsAcc<Cv, RG> acc;
     acc.zero();
     unsigned phase = 0;
-    for (int i = j; i < nb; ++i) {
-        const int st = (i - j) & 1;
+    for (int i = i0; i <= i1; ++i) {
+        const int st = (i - i0) & 1;
         if (!__syncthreads_and(bar_wait(&bar[st], (phase >> st) & 1u, status))) return;
         phase ^= 1u << st;
         const Cv* tile = stage(st);
@@ -598,23 +650,34 @@ __global__ void __launch_bounds__(256, 1) k_bwd_inv_diag(const SolveBlockTask* _
                 const int c = cpart * RPT + ((u0 + q + ccol) & (RPT - 1));
                 acc.add(q, tile[c + ccol * SB], gb + c * RS);
             }
-        if (i + 1 < nb) pf.commit(gbuf(st ^ 1));
-        if (i + 2 < nb) fetch(i + 2);
+        if (i + 1 <= i1) pf.commit(gbuf(st ^ 1));
+        if (i + 2 <= i1) fetch(i + 2);
         __syncthreads();
-        if (i + 2 < nb) issue(i + 2);
+        if (i + 2 <= i1) issue(i + 2);
     }
     acc.store(part + (cpart * SB + ccol) * RG);
     __syncthreads();
+    Cv x[FG];
+#pragma unroll
+    for (int q = 0; q < FG; ++q) {
+        const int g = g0 + q;
+        x[q] = Cv(0);
+        if (fin && g < ng) {
+            x[q] = part[ccol * RG + g];
+#pragma unroll
+            for (int p = 1; p < TPC; ++p) x[q] += part[(p * SB + ccol) * RG + g];
+        }
+    }
+    if (!inv_chunk_combine<Cv, SB, FG>(x, fin, ccol, g0, ng, rg, A.nrhs, tk.r1, (i0 - j) / kInvDiagChunk, tk.flags,
+                                       pbuf, cnt))
+        return;
     if (fin) {
         const int kn = min(SB, d.w - j * SB);
 #pragma unroll
         for (int q = 0; q < FG; ++q) {
             const int g = g0 + q;
             if (g >= ng || ccol >= kn) break;
-            Cv x = part[ccol * RG + g];
-#pragma unroll
-            for (int p = 1; p < TPC; ++p) x += part[(p * SB + ccol) * RG + g];
-            work[d.first_col + j * SB + ccol + (long long)(rg + g) * A.ldw] = x;
+            work[d.first_col + j * SB + ccol + (long long)(rg + g) * A.ldw] = x[q];
         }
     }
 }

@@ -594,11 +594,21 @@ Plan build_from_fronts(int n, int count, const int* first_column, const int* par
         if (!inv.empty()) {
             // y_1 per block row, then the trailing rows in chunks of SB - A rows (the tile copy starts
             // at the chunk's first row rounded down to 16 bytes)
-            int b = (int)P.solve_tasks.size();
+            int b = (int)P.solve_tasks.size(), dslots = 0;
             for (int s : inv) {
                 const int nb = (P.sn[s].w + SB - 1) / SB;
-                for (int i = 0; i < nb; ++i) P.solve_tasks.push_back({s, i, nb, inv_ob[s], 0, 0, first_blk[s]});
+                for (int i = 0; i < nb; ++i) {
+                    const int nc = (i + kInvDiagChunk) / kInvDiagChunk;   // blocks 0 .. i
+                    for (int c = 0; c < nc; ++c) {
+                        SolveBlockTask t{s, i, nb, inv_ob[s], dslots, nc, first_blk[s]};
+                        t.c0 = c * kInvDiagChunk;
+                        t.c1 = std::min(i, t.c0 + kInvDiagChunk - 1);
+                        P.solve_tasks.push_back(t);
+                    }
+                    dslots += nc;
+                }
             }
+            P.inv_diag_slots = std::max(P.inv_diag_slots, dslots);
             P.fwd_launches.push_back(simple(SolveLaunch::FwdInvDiag, b));
             b = (int)P.solve_tasks.size();
             const int height = SB - kTileAlignRows(cfg);
@@ -652,7 +662,7 @@ Plan build_from_fronts(int n, int count, const int* first_column, const int* par
         if (!inv.empty()) {
             // partial sums per (column block, chunk of kInvColRowsPlan trailing rows), their sums
             // per column block in chunk order, then x_1 per block column
-            int b = (int)P.solve_tasks.size(), slots = 0;
+            int b = (int)P.solve_tasks.size(), slots = 0, dslots = 0;
             std::vector<SolveBlockTask> diag_tasks, reduce_tasks;
             for (int s : inv) {
                 const SnDev& d = P.sn[s];
@@ -665,7 +675,16 @@ Plan build_from_fronts(int n, int count, const int* first_column, const int* par
                     }
                 if (nq > 0)
                     for (int kb = 0; kb < nb; ++kb) reduce_tasks.push_back({s, kb, nb, slots + kb * nq, nq, 0, 0});
-                for (int j = 0; j < nb; ++j) diag_tasks.push_back({s, j, nb, inv_ob[s], 0, 0, first_blk[s]});
+                for (int j = 0; j < nb; ++j) {
+                    const int nc = (nb - j + kInvDiagChunk - 1) / kInvDiagChunk;   // blocks j .. nb-1
+                    for (int c = 0; c < nc; ++c) {
+                        SolveBlockTask t{s, j, nb, inv_ob[s], dslots, nc, first_blk[s]};
+                        t.c0 = j + c * kInvDiagChunk;
+                        t.c1 = std::min(nb - 1, t.c0 + kInvDiagChunk - 1);
+                        diag_tasks.push_back(t);
+                    }
+                    dslots += nc;
+                }
                 slots += nb * nq;
             }
             if ((int)P.solve_tasks.size() > b) P.bwd_launches.push_back(simple(SolveLaunch::BwdInvCols, b));
@@ -675,6 +694,7 @@ Plan build_from_fronts(int n, int count, const int* first_column, const int* par
                 P.bwd_launches.push_back(simple(SolveLaunch::BwdInvReduce, b));
             }
             P.inv_partial_slots = std::max(P.inv_partial_slots, slots);
+            P.inv_diag_slots = std::max(P.inv_diag_slots, dslots);
             b = (int)P.solve_tasks.size();
             P.solve_tasks.insert(P.solve_tasks.end(), diag_tasks.begin(), diag_tasks.end());
             P.bwd_launches.push_back(simple(SolveLaunch::BwdInvDiag, b));

@@ -19,6 +19,7 @@ constexpr int kInvColRowsPlan = 1024;   // trailing rows per backward partial-su
 constexpr int kDefaultInvCols = 2048;   // widest front whose diagonal block is kept inverted for the solves
 constexpr int kSuperBlocks = 4;       // tensor-core path: outer blocks per super-block of the own-column updates
 constexpr int kDefaultMergeCols = 2048;   // widest device front made of a chain of supernodes (merge_chains)
+constexpr int kInvDiagChunk = 2;         // inverse blocks per task of the inverse-front diagonal products
 
 struct PlanConfig {
     int pivot_block = 32;     // FP64 pivot block (the reference's PanelWidth)
@@ -85,12 +86,15 @@ struct SolveLaunch {
 // at block index ob_s + i (i - 1) / 2 + j of the off-diagonal arena.  Tasks:
 //   inversion            {s, i, j, ob_s, -, -, blk}: block (i, j) from the blocks
 //                        (k, j), j <= k < i (launched by diagonal i - j);
-//   FwdInvDiag           {s, i, nb, ob_s, -, -, blk}: y_i = sum_{j <= i} Linv(i, j) f_j;
+//   FwdInvDiag           {s, i, nb, ob_s, slot0, nc, blk, j0, j1}: the part j0 <= j <= j1 of
+//                        y_i = sum_{j <= i} Linv(i, j) f_j; block row i is split in nc chunks of
+//                        kInvDiagChunk blocks (partial slots slot0 .. slot0+nc-1; nc = 1: no split);
 //   FwdInvTail           {s, -, nb, r0, r1, -, -}: f[r0, r1) -= L[r0:r1, 0:w] y;
 //   BwdInvCols           {s, kb, nb, r0, r1, -, slot}: partial sums of L[r0:r1, block kb]^T g
 //                        into partial slot `slot` (a block's nq chunks have consecutive slots);
 //   BwdInvReduce         {s, kb, nb, slot0, nq, -, -}: g of block kb -= its nq partial sums;
-//   BwdInvDiag           {s, j, nb, ob_s, -, -, blk}: x_j = sum_{i >= j} Linv(i, j)^T g_i.
+//   BwdInvDiag           {s, j, nb, ob_s, slot0, nc, blk, i0, i1}: the part i0 <= i <= i1 of
+//                        x_j = sum_{i >= j} Linv(i, j)^T g_i, in chunks as FwdInvDiag.
 // blk is the diagonal-inverse index of the front's block 0.
 struct InvLaunch {
     int begin, count;   // inversion tasks of one diagonal i - j
@@ -105,6 +109,7 @@ struct InvLaunch {
 struct SolveBlockTask {
     int s, k0, kn, r0, r1;
     int flags, blk;
+    int c0 = 0, c1 = 0;   // inverse-front diagonal tasks: the range of inverse blocks summed
 };
 
 // Host mirror of the device TcJob (tc_gemm.cuh): one rank-kn update of a front.
@@ -167,6 +172,7 @@ struct Plan {
     std::vector<InvLaunch> inv_launches;
     long long inv_off_blocks = 0;              // blocks of the off-diagonal inverse arena
     int inv_partial_slots = 0;                 // most BwdInvCols partial slots of one launch (SB x nrhs each)
+    int inv_diag_slots = 0;                    // most inverse-diagonal partial slots of one launch (SB x nrhs each)
     int progress_count = 0;                    // progress counters of all level launches
     int bwd_partial_slots = 0;                 // most backward column-dot partial slots of one launch (8 x nrhs each)
 };
