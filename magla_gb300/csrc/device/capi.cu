@@ -171,7 +171,7 @@ struct uchol_symbolic_s {
                           std::to_string(c.small_mask) + "/" + std::to_string(c.tensor_core) + "/" +
                           std::to_string(c.solve_block) + "/" + std::to_string(c.merge_cols) + "/" +
                           std::to_string(c.merge_fill) + "/" + std::to_string(c.inv_cols) + "/" +
-                          std::to_string(c.side_extend_add);
+                          std::to_string(c.side_extend_add) + "/" + std::to_string(c.sms);
         auto it = plans.find(key);
         if (it != plans.end()) {
             check_budget(budget, planned_bytes(it->second->plan, precision, nnz, full_nnz, n));
@@ -738,12 +738,13 @@ uchol_factor_s* create_factor(uchol_symbolic_s* S, int n, int nnz, const uchol_o
     F->precision = F->opts.precision;
     F->elem = F->precision == UCHOL_PRECISION_FP64 ? 8 : 4;
     PlanConfig cfg = config_for(F->opts);
+    CK(cudaDeviceGetAttribute(&F->sms, cudaDevAttrMultiProcessorCount, S->device));
+    cfg.sms = F->sms;
     F->dp = S->get_plan(cfg, F->precision, F->opts.device_memory_budget);
     const Plan& P = F->dp->plan;
     cudaStream_t st = S->stream;
     F->panel.alloc((size_t)P.factor_elems * F->elem, "factor panels");
     F->contrib.alloc((size_t)P.contrib_elems * F->elem, "contribution blocks");
-    CK(cudaDeviceGetAttribute(&F->sms, cudaDevAttrMultiProcessorCount, S->device));
     bool side = false;
     for (const Launch& L : P.launches) side |= L.stream == 1;
     if (side) {

@@ -660,18 +660,28 @@ Plan build_from_fronts(int n, int count, const int* first_column, const int* par
         if (solo.count > 0) P.bwd_launches.push_back(solo);
         if (!multi.empty()) P.bwd_launches.push_back(level_launch(SolveLaunch::BwdLevel, multi, false));
         if (!inv.empty()) {
-            // partial sums per (column block, chunk of kInvColRowsPlan trailing rows), their sums
-            // per column block in chunk order, then x_1 per block column
+            // partial sums per (column block, chunk of trailing rows), their sums per column block
+            // in chunk order, then x_1 per block column.  With the SM count known, the level's
+            // trailing rows are cut into as many chunks as make at most two tasks per SM (one
+            // round of the two CTAs an SM holds); otherwise chunks of kInvColRowsPlan rows.
             int b = (int)P.solve_tasks.size(), slots = 0, dslots = 0;
             std::vector<SolveBlockTask> diag_tasks, reduce_tasks;
+            int level_blocks = 0;
+            for (int s : inv) level_blocks += (P.sn[s].w + SB - 1) / SB;
             for (int s : inv) {
                 const SnDev& d = P.sn[s];
                 const int nb = (d.w + SB - 1) / SB;
-                const int nq = (d.m - d.w + kInvColRowsPlan - 1) / kInvColRowsPlan;
+                const int t = d.m - d.w;
+                int nq = (t + kInvColRowsPlan - 1) / kInvColRowsPlan, height = kInvColRowsPlan;
+                if (cfg.sms > 0 && t > 0) {
+                    nq = std::max(1, std::min((t + SB / 2 - 1) / (SB / 2), 2 * cfg.sms / std::max(1, level_blocks)));
+                    height = (t + nq - 1) / nq;
+                    nq = (t + height - 1) / height;
+                }
                 for (int kb = 0; kb < nb; ++kb)
                     for (int q = 0; q < nq; ++q) {
-                        const int r0 = d.w + q * kInvColRowsPlan;
-                        P.solve_tasks.push_back({s, kb, nb, r0, std::min(d.m, r0 + kInvColRowsPlan), 0, slots + kb * nq + q});
+                        const int r0 = d.w + q * height;
+                        P.solve_tasks.push_back({s, kb, nb, r0, std::min(d.m, r0 + height), 0, slots + kb * nq + q});
                     }
                 if (nq > 0)
                     for (int kb = 0; kb < nb; ++kb) reduce_tasks.push_back({s, kb, nb, slots + kb * nq, nq, 0, 0});

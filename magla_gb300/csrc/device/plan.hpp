@@ -35,6 +35,7 @@ struct PlanConfig {
     double merge_fill = 0.05; // largest growth of the stored entries a grouping may cost
     bool side_extend_add = false;   // tensor-core path: the extend-add into the contribution columns of
                                     // large fronts runs on a second stream, beside the level's outer blocks
+    int sms = 0;                    // > 0: the device's SM count (sizes the backward inverse-front chunks)
 };
 
 // Device fronts from the supernode partition: runs of supernodes in which each
