@@ -353,6 +353,7 @@ int uchol_line_cross_plan_create(uchol_dmatrix m, int count, const int* indices,
  * values only. */
 int uchol_line_cross(uchol_dmatrix m, uchol_values_plan p, double* rhs, int ldr, int nrhs, const double* prescribed,
                      int ldp, int on_device);
+/* Plans and their matrix may be destroyed in either order. */
 int uchol_values_plan_destroy(uchol_values_plan p);
 /* y = A x in FP64 (nrhs columns). */
 int uchol_dmatrix_multiply(uchol_dmatrix m, int nrhs, const double* x, int ldx, double* y, int ldy, int on_device);

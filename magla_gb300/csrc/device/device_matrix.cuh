@@ -33,7 +33,7 @@ struct uchol_dmatrix_s {
 };
 
 struct uchol_values_plan_s {
-    uchol_dmatrix_s* m = nullptr;
+    uchol_dmatrix_s* m = nullptr;   // compared, never dereferenced after creation
     int kind = 0;   // 0: AccumulateAt list, 1: LineCross list
     int count = 0;
     // AccumulateAt: targets (distinct positions, ascending) and their items in list order
@@ -806,9 +806,11 @@ int uchol_line_cross(uchol_dmatrix m, uchol_values_plan p, double* rhs, int ldr,
 }
 
 int uchol_values_plan_destroy(uchol_values_plan p) {
+    // The plan's matrix may already be destroyed (the two are released in any order): the
+    // plan only keeps its address for the check that it is applied to that matrix, and is
+    // freed without touching it (cudaFree waits for the device work that reads the buffers).
     return guarded([&] {
         if (!p) return;
-        if (p->m && p->m->stream) cudaStreamSynchronize(p->m->stream);
         delete p;
     });
 }

@@ -23,6 +23,7 @@ reference's sequential calls give, bit for bit.
 from __future__ import annotations
 
 import ctypes as C
+import sys
 
 import numpy as np
 
@@ -151,7 +152,9 @@ class DeviceSymmetricCSRMatrix:
         self._h = None
 
     def __del__(self):
-        self.close()
+        # at interpreter exit the CUDA context goes away with the process: no call into it
+        if not sys.is_finalizing():
+            self.close()
 
 
 class _Plan:
@@ -161,7 +164,7 @@ class _Plan:
 
     def __del__(self):
         h = getattr(self, "_h", None)
-        if h is not None and _native._GPU is not None:
+        if h is not None and _native._GPU is not None and not sys.is_finalizing():
             _native._GPU.uchol_values_plan_destroy(h)
         self._h = None
 

@@ -26,6 +26,7 @@ import enum
 import hashlib
 import json
 import os
+import sys
 
 import numpy as np
 
@@ -287,7 +288,8 @@ class UtduSymbolicFactorization:
 
     def __del__(self):
         h = getattr(self, "_device", None)
-        if h is not None and _native._GPU is not None:
+        # at interpreter exit the CUDA context goes away with the process: no call into it
+        if h is not None and _native._GPU is not None and not sys.is_finalizing():
             _native._GPU.uchol_symbolic_destroy(h)
             self._device = None
 
@@ -501,7 +503,7 @@ class UtduNumericFactorization:
 
     def __del__(self):
         h = getattr(self, "_h", None)
-        if h is not None and _native._GPU is not None:
+        if h is not None and _native._GPU is not None and not sys.is_finalizing():
             _native._GPU.uchol_factor_destroy(h)
             self._h = None
 

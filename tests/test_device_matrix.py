@@ -267,3 +267,41 @@ def test_pcg_failures(gpu_lib):
     s = ConjugateGradientGaussPreSolver(RelativeTolerance=1e-14, MaxIterations=3)
     s.Solve(LinearSystem(m, build_vector(m.Size, 1)))
     assert s.LastResult.Iterations == 3 and not s.LastResult.Converged
+
+
+def test_plan_outlives_its_matrix(gpu_lib):
+    """A plan and its matrix are released in either order."""
+    m = _build(3, [(0, 0, 4.0), (0, 1, 2.0), (1, 1, 5.0), (2, 2, 9.0)])
+    dm = DeviceSymmetricCSRMatrix(m)
+    p = dm.AccumulatePlan([0, 1], [1, 1])
+    q = dm.LineCrossPlan([2])
+    dm.close()
+    del p, q
+    dm2 = DeviceSymmetricCSRMatrix(m)
+    assert np.array_equal(dm2.Values, m.Values)
+
+
+def test_process_exit_with_live_handles(gpu_lib, tmp_path):
+    """A script that keeps matrices, plans and factors in module globals exits cleanly."""
+    import subprocess
+    import sys
+    from pathlib import Path
+    root = Path(__file__).resolve().parent.parent
+    script = tmp_path / "live.py"
+    script.write_text(
+        "import sys\n"
+        f"sys.path.insert(0, {str(root)!r})\n"
+        "import numpy as np\n"
+        "import magla_gb300 as mg\n"
+        "from magla_gb300 import generators as G\n"
+        "m = G.laplacian3d(6, 6, 6)\n"
+        "dm = mg.DeviceSymmetricCSRMatrix(m)\n"
+        "p = dm.AccumulatePlan([0], [0])\n"
+        "q = dm.LineCrossPlan([1])\n"
+        "f = mg.SymmetricUtduSolver().Factorize(m)\n"
+        "f.RefactorizeFrom(dm)\n"
+        "x = mg.ConjugateGradientGaussPreSolver().Solve(mg.LinearSystem(m, np.ones(m.Size)))\n"
+        "print('done')\n")
+    r = subprocess.run([sys.executable, str(script)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, (r.returncode, r.stderr[-2000:])
+    assert "done" in r.stdout
