@@ -126,3 +126,18 @@ def test_oracle_matches_host_container_bit_for_bit():
         m.LineCross(h, float(pres[t]), int(idx[t]))
     assert np.array_equal(m.Values, vals)
     assert np.array_equal(h, rhs)
+
+
+def test_device_cg_argument_checks_without_a_gpu():
+    """The Jacobi-PCG mirror validates its arguments before any device call
+    (ConjugateGradientGaussPreSolver.cs:78-101, IterativeLinearSolver.cs:26-33)."""
+    from magla_gb300 import (ArgumentException, ArgumentOutOfRangeException, ConjugateGradientGaussPreSolver,
+                             LinearSystem)
+    m = _diagonal([2.0, 3.0])
+    with pytest.raises(ArgumentOutOfRangeException) as e:
+        ConjugateGradientGaussPreSolver(MaxIterations=-1).Solve(LinearSystem(m, [1.0, 1.0]))
+    assert e.value.ParamName == "MaxIterations"
+    with pytest.raises(ArgumentOutOfRangeException):
+        ConjugateGradientGaussPreSolver(RelativeTolerance=-1.0).Solve(LinearSystem(m, [1.0, 1.0]))
+    with pytest.raises(ArgumentException):
+        ConjugateGradientGaussPreSolver().SolveWithInitialGuess(LinearSystem(m, [1.0, 1.0]), [1.0])
