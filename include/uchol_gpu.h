@@ -388,6 +388,15 @@ int uchol_jacobi_pcg(uchol_dmatrix m, int nrhs, const double* b, int ldb, double
  * m's stream; the values do not leave the device. */
 int uchol_refactorize_dmatrix(uchol_factor f, uchol_dmatrix m, uchol_factor_stats* stats);
 
+/* Plan check (host only, no GPU needed): builds the execution plan of `desc` for the options
+ * and an SM count (0 = unknown) and verifies the invariants its launches rely on (every
+ * received column assembled once, side-stream launches joined, solve chunks tiling their
+ * rows and blocks with distinct partial slots).  UCHOL_INTERNAL with the violated invariant
+ * in uchol_last_error.  counts (optional, 5 ints): extend-add items, side-stream launches,
+ * inverse-diagonal rows split in chunks, backward row chunks, forward trailing-row chunks.
+ * No counterpart in the reference. */
+int uchol_check_plan(const uchol_symbolic_desc* desc, const uchol_options* opts, int sms, int* counts);
+
 /* Number of kernel launches this library has issued since it was loaded. */
 int64_t uchol_kernel_launches(void);
 /* Per-phase device timing of factorisations (one CUDA event pair per launch);

@@ -172,6 +172,7 @@ GPU_SYMBOLS = {
                                            C.POINTER(C.c_int64), c_int_p]),
     "uchol_check_diag_panel": (C.c_int, [C.c_int, C.c_int, C.c_void_p, C.c_double, C.c_double, C.c_int, C.c_void_p,
                                          C.c_void_p, C.c_void_p, c_int_p]),
+    "uchol_check_plan": (C.c_int, [C.POINTER(SymbolicDesc), C.POINTER(Options), C.c_int, c_int_p]),
     "uchol_set_wait_limits": (C.c_int, [C.c_double, C.c_double]),
     "uchol_check_solve_wait": (C.c_int, [C.c_void_p, C.c_double]),
     "uchol_dmatrix_create": (C.c_int, [C.c_int, C.c_int, c_int_p, c_int_p, C.c_void_p, C.c_void_p, c_void_pp]),

@@ -218,4 +218,146 @@ int uchol_check_diag_panel(int m, int nb, const float* front, double threshold, 
     });
 }
 
+
+// Plan check (host only): builds the execution plan of a symbolic factorisation for the
+// given options and SM count and verifies the invariants its launches rely on; no GPU needed.
+int uchol_check_plan(const uchol_symbolic_desc* d, const uchol_options* opts, int sms, int* counts) {
+    return guarded([&] {
+        // counts (optional, 5 ints): extend-add items, side-stream launches, inverse-diagonal rows
+        // split in more than one chunk, backward row chunks, forward trailing-row chunks
+        int n_items = 0, n_side = 0, n_split = 0, n_bchunks = 0, n_fchunks = 0;
+        if (!d) throw Error(UCHOL_BAD_ARG, "null argument");
+        check_options(opts);
+        uchol_options o;
+        if (opts) o = *opts; else uchol_default_options(&o);
+        PlanConfig cfg = config_for(o);
+        cfg.sms = sms;
+        Plan P;
+        try {
+            P = build_plan(d->n, d->supernode_count, d->first_column, d->parent, d->child_ptr, d->children,
+                           d->front_ptr, d->front_rows, d->diag_value_index, d->pattern_ptr, d->pattern_rows,
+                           d->lower_start, d->lower_value_ptr, d->lower_value_index, d->nnz, cfg);
+        } catch (const std::runtime_error& e) {
+            throw Error(UCHOL_BAD_ARG, std::string("inconsistent symbolic factorization: ") + e.what());
+        }
+        auto fail = [](const std::string& m) { throw Error(UCHOL_INTERNAL, "plan check: " + m); };
+        // (1) extend-add: every receiving column of a front with children exactly once; side-stream
+        //     items only for the contribution columns of fronts not factorised whole; a side launch
+        //     is joined by the next contribution update before another one forks
+        std::map<std::pair<int, int>, int> seen;
+        bool pending = false;
+        for (const Launch& L : P.launches) {
+            if (L.kind == Launch::ExtendAdd) n_items += L.count;
+            if (L.stream == 1) ++n_side;
+            if (L.kind == Launch::ExtendAdd)
+                for (int q = L.begin; q < L.begin + L.count; ++q) {
+                    const EaItem& it = P.ea_items[q];
+                    const SnDev& pd = P.sn[it.parent];
+                    if (++seen[{it.parent, it.pcol}] != 1) fail("a receiving column appears twice");
+                    if (L.stream == 1 && (it.pcol < pd.w || small_front(P.cfg, pd.m)))
+                        fail("a side-stream extend-add item outside the contribution columns of a large front");
+                    for (int e = it.begin; e < it.end; ++e)
+                        if (e < 0 || e >= (int)P.ea_entries.size()) fail("extend-add entry out of range");
+                }
+            if (L.stream == 1) {
+                if (pending) fail("a side launch forks before the previous one is joined");
+                pending = true;
+            } else if (L.stream == 2) {
+                if (!pending) fail("a join without a side launch");
+                if (L.kind != Launch::TcUpdate) fail("a join on a launch other than a contribution update");
+                for (int j = L.begin; j < L.begin + L.count; ++j) {
+                    const TcJobHost& J = P.tc_jobs[j];
+                    if (J.c0 != P.sn[J.s].w || J.kbeg != 0 || J.kn != P.sn[J.s].w) fail("the join is not a contribution update");
+                }
+                pending = false;
+            }
+        }
+        if (pending) fail("a side launch is never joined");
+        for (int s = 0; s < P.count; ++s) {
+            const SnDev& sd = P.sn[s];
+            if (sd.parent < 0) continue;
+            for (int a = 0; a < sd.m - sd.w; ++a)
+                if (!seen.count({sd.parent, P.rel[sd.rel_off + a]})) fail("a child's trailing row is not received");
+        }
+        // (2) solve tasks
+        const int SB = P.cfg.solve_block;
+        auto check_chunks = [&](const SolveLaunch& L, bool fwd) {
+            std::map<std::pair<int, int>, std::vector<const SolveBlockTask*>> rows;
+            std::map<int, int> slots;
+            for (int q = L.begin; q < L.begin + L.count; ++q) {
+                const SolveBlockTask& t = P.solve_tasks[q];
+                rows[{t.s, t.k0}].push_back(&t);
+            }
+            for (auto& kv : rows) {
+                const int lo = fwd ? 0 : kv.first.second;
+                const int hi = fwd ? kv.first.second : kv.second[0]->kn - 1;
+                int next = lo;
+                const int nc = (int)kv.second.size();
+                n_split += nc > 1;
+                for (const SolveBlockTask* t : kv.second) {
+                    if (t->c0 != next || t->c1 < t->c0 || t->c1 - t->c0 + 1 > kInvDiagChunk) fail("diagonal chunks do not tile the row");
+                    if (t->flags != nc || t->r1 != kv.second[0]->r1) fail("diagonal chunk count or slot base differs");
+                    const int slot = t->r1 + (t->c0 - lo) / kInvDiagChunk;
+                    if (slot >= std::max(1, P.inv_diag_slots) || ++slots[slot] != 1) fail("diagonal chunk slot reused or out of range");
+                    next = t->c1 + 1;
+                }
+                if (next != hi + 1) fail("diagonal chunks do not reach the row's end");
+            }
+        };
+        for (const SolveLaunch& L : P.fwd_launches) {
+            if (L.kind == SolveLaunch::FwdInvDiag) check_chunks(L, true);
+            if (L.kind == SolveLaunch::FwdInvTail) {
+                std::map<int, std::vector<std::pair<int, int>>> rr;
+                for (int q = L.begin; q < L.begin + L.count; ++q)
+                    rr[P.solve_tasks[q].s].push_back({P.solve_tasks[q].r0, P.solve_tasks[q].r1});
+                for (auto& kv : rr) {
+                    std::sort(kv.second.begin(), kv.second.end());
+                    int next = P.sn[kv.first].w;
+                    for (auto& r : kv.second) {
+                        ++n_fchunks;
+                        if (r.first != next || r.second <= r.first || r.second - r.first > SB) fail("forward tail chunks do not tile the rows");
+                        next = r.second;
+                    }
+                    if (next != P.sn[kv.first].m) fail("forward tail chunks do not reach the front's end");
+                }
+            }
+        }
+        for (size_t li = 0; li < P.bwd_launches.size(); ++li) {
+            const SolveLaunch& L = P.bwd_launches[li];
+            if (L.kind == SolveLaunch::BwdInvDiag) check_chunks(L, false);
+            if (L.kind == SolveLaunch::BwdInvCols) {
+                std::map<std::pair<int, int>, std::vector<const SolveBlockTask*>> cols;
+                std::map<int, int> slots;
+                for (int q = L.begin; q < L.begin + L.count; ++q) cols[{P.solve_tasks[q].s, P.solve_tasks[q].k0}].push_back(&P.solve_tasks[q]);
+                for (auto& kv : cols) {
+                    int next = P.sn[kv.first.first].w;
+                    for (const SolveBlockTask* t : kv.second) {
+                        ++n_bchunks;
+                        if (t->r0 != next || t->r1 <= t->r0) fail("backward chunks do not tile the rows");
+                        if (t->blk >= std::max(1, P.inv_partial_slots) || ++slots[t->blk] != 1) fail("backward chunk slot reused or out of range");
+                        next = t->r1;
+                    }
+                    if (next != P.sn[kv.first.first].m) fail("backward chunks do not reach the front's end");
+                }
+                if (li + 1 >= P.bwd_launches.size() || P.bwd_launches[li + 1].kind != SolveLaunch::BwdInvReduce)
+                    fail("backward chunks without their reduction");
+                const SolveLaunch& R = P.bwd_launches[li + 1];
+                for (int q = R.begin; q < R.begin + R.count; ++q) {
+                    const SolveBlockTask& t = P.solve_tasks[q];
+                    auto it = cols.find({t.s, t.k0});
+                    if (it == cols.end() || t.r1 != (int)it->second.size() || t.r0 != it->second[0]->blk)
+                        fail("a reduction does not match its chunks");
+                }
+            }
+        }
+        if (counts) {
+            counts[0] = n_items;
+            counts[1] = n_side;
+            counts[2] = n_split;
+            counts[3] = n_bchunks;
+            counts[4] = n_fchunks;
+        }
+    });
+}
+
 }  // extern "C"
