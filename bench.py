@@ -242,10 +242,12 @@ def run_ours(args):
     d_x = torch.zeros_like(d_b)
     bnorm = np.linalg.norm(_cols(b), axis=0)
 
-    # ---- plain FP64 GPU arm: factorisation (device time; graph capture excluded) + one solve
+    # ---- plain FP64 GPU arm: factorisation (device time; graph capture excluded) + one solve;
+    # measured at N = 1 only (N > 1 runs replicas of the same step, and the arm holds every GPU
+    # for minutes)
     fp64 = None
     x64 = None
-    if not args.no_fp64 and prec != mg.Precision.FP64:
+    if not args.no_fp64 and prec != mg.Precision.FP64 and world == 1:
         s64 = mg.SymmetricUtduSolver(mg.UtduSolverOptions(Ordering=ordering, Precision=mg.Precision.FP64,
                                                           ChainMergeWidth=args.chain_merge_width))
         f64 = s64.FactorizeDevice(m, sym, d_sets[0].data_ptr())
@@ -341,7 +343,7 @@ def run_ours(args):
     traffic = gemm_traffic(args, prec)
     if rank != 0:
         return
-    cb = None if args.no_cpu_baseline else cpu_baseline(args, os.cpu_count() or 1)
+    cb = None if (args.no_cpu_baseline or world > 1) else cpu_baseline(args, os.cpu_count() or 1)
     value = world * ops / (ms / 1e3) / 1e12
     entries = sym.FactorEntryCount
     apps = [it + 1 for it in iters]   # factor applications per refined solve (x0 plus one per step)
