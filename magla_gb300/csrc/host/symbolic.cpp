@@ -280,8 +280,14 @@ Supernodes build_supernodes(const PermutedPattern& pattern, const std::vector<in
                     throw std::runtime_error("symbolic phase: front size prediction exceeded (internal error)");
                 sn.pattern_rows[write++] = r;
             }
+        // the rows so far in any order; each child's trailing rows follow as a segment in its
+        // own (ascending) order, so the distinct rows are sorted by one small sort and a merge
+        // per child instead of a sort of the whole front
+        auto base = sn.pattern_rows.begin() + sn.pattern_ptr[s];
+        std::sort(base, sn.pattern_rows.begin() + write);
         for (int c = sn.child_ptr[s]; c < sn.child_ptr[s + 1]; ++c) {
             int child = sn.children[c];
+            const int seg = write;
             for (int q = sn.pattern_ptr[child] + sn.width(child); q < sn.pattern_ptr[child + 1]; ++q) {
                 int r = sn.pattern_rows[q];
                 if (flag[r] == s) continue;
@@ -290,11 +296,11 @@ Supernodes build_supernodes(const PermutedPattern& pattern, const std::vector<in
                     throw std::runtime_error("symbolic phase: front size prediction exceeded (internal error)");
                 sn.pattern_rows[write++] = r;
             }
+            std::inplace_merge(base, sn.pattern_rows.begin() + seg, sn.pattern_rows.begin() + write);
         }
         if (write != sn.pattern_ptr[s + 1])
             throw std::runtime_error("symbolic phase: predicted front size of supernode " + std::to_string(s) +
                                      " does not match the actual one (internal error)");
-        std::sort(sn.pattern_rows.begin() + sn.pattern_ptr[s], sn.pattern_rows.begin() + sn.pattern_ptr[s + 1]);
     }
 
     // Costs and the exact peak of live contribution blocks (SupernodalStructure.cs:370-418).
