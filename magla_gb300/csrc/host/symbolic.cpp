@@ -381,9 +381,20 @@ Symbolic analyze_ordered(int n, const int* row_ptr, const int* col, int nnz, con
     S.permutation.resize(n);
     for (int k = 0; k < n; ++k) S.permutation[k] = fill_reducing[post[k]];
     S.inverse_permutation = invert(S.permutation);
-    S.pattern = permute_pattern(n, row_ptr, col, S.inverse_permutation);
-    S.etree_parent = etree_build(n, S.pattern.ptr, S.pattern.rows);
-    std::vector<int> final_post = etree_postorder(n, S.etree_parent);
+    std::vector<int> final_post;
+    bool post_is_identity = true;
+    for (int k = 0; k < n && post_is_identity; ++k) post_is_identity = post[k] == k;
+    if (post_is_identity) {
+        // the order is already a postorder (a chain, for instance): the second pass would
+        // rebuild the same pattern, tree and postorder
+        S.pattern = std::move(first_pattern);
+        S.etree_parent = std::move(first_parent);
+        final_post = std::move(post);
+    } else {
+        S.pattern = permute_pattern(n, row_ptr, col, S.inverse_permutation);
+        S.etree_parent = etree_build(n, S.pattern.ptr, S.pattern.rows);
+        final_post = etree_postorder(n, S.etree_parent);
+    }
     S.column_counts = etree_column_counts(n, S.pattern.ptr, S.pattern.rows, S.etree_parent, final_post);
     S.supernodes = build_supernodes(S.pattern, S.etree_parent, S.column_counts, std::max(1, amalgamation_limit));
     for (int j = 0; j < n; ++j) S.strict_factor_nonzero_count += S.column_counts[j];
