@@ -371,3 +371,18 @@ def test_solve_into_caller_buffer(gpu_lib, prec):
     assert np.array_equal(x1, f.Solve(B[:, 0].copy()))
     with pytest.raises(ArgumentException):
         f.Solve(B, out=np.zeros((m.Size, 2)))   # row-major block
+
+
+@pytest.mark.gpu
+def test_many_rhs_through_inverse_fronts(gpu_lib):
+    """33 right-hand sides (three groups of 16 in the trailing-row kernels, five of 8 in the
+    inverse-diagonal products) on a natural-order chain of inverse fronts: each column equals
+    its own one-column solve to the FP32 accuracy of the factor's application."""
+    m = G.elasticity(10, 10, 5)[0]
+    opts = UtduSolverOptions(Ordering=FillReducingOrdering.Natural, Precision=Precision.TF32)
+    f = SymmetricUtduSolver(opts).Factorize(m)
+    B = np.asfortranarray(np.stack([build_vector(m.Size, 200 + k) for k in range(33)], axis=1))
+    X = f._apply(B)
+    for k in (0, 15, 16, 31, 32):
+        xk = f._apply(B[:, k].copy())
+        assert max_relative_difference(X[:, k], xk) < 1e-5, k
