@@ -148,14 +148,20 @@ def test_pivot_range_and_diagonal_against_dense_ldlt():
 
 def test_grid_solution_agrees_with_conjugate_gradients():
     """Tests/UCHOL/SymmetricUtduSolverTests.cs:309-328: the direct solution of the grid 7^3
-    (2 unknowns per node) agrees with an iterative CG solution to 1e-6.  MAGLA's own CG
-    solver is outside this build, so scipy's CG on the same matrix stands in for it.  The
-    right-hand side uses the cited test's seed, 11; the vector generator is this build's."""
-    spla = pytest.importorskip("scipy.sparse.linalg")
+    (2 unknowns per node) agrees with the Jacobi-PCG solution (RelativeTolerance 1e-12,
+    MaxIterations 20000) to 1e-6: the oracle's restatement of MAGLA's
+    ConjugateGradientGaussPreSolver (oracle/oracle_values.cpp), and scipy's CG as a second,
+    independent iterative solver.  The right-hand side uses the cited test's seed, 11; the
+    vector generator is this build's."""
     m = G.grid_matrix(7, 7, 7, 2)
     b = build_vector(m.Size, 11)
     _, f = factor(m)
     x = f.Solve(b)
+    xj, _, converged, _, _ = oracle.jacobi_pcg(m, b, tolerance=1e-12, max_iterations=20000)
+    assert converged
+    assert max_relative_difference(x, xj) < 1e-6
+    assert relative_residual(m, b, x) < 1e-12
+    spla = pytest.importorskip("scipy.sparse.linalg")
     A = spla.LinearOperator((m.Size, m.Size), matvec=m.Multiply, dtype=np.float64)
     try:
         xc, info = spla.cg(A, b, rtol=1e-12, atol=0.0, maxiter=20 * m.Size)
@@ -163,4 +169,3 @@ def test_grid_solution_agrees_with_conjugate_gradients():
         xc, info = spla.cg(A, b, tol=1e-12, atol=0.0, maxiter=20 * m.Size)
     assert info == 0
     assert max_relative_difference(x, xc) < 1e-6
-    assert relative_residual(m, b, x) < 1e-12
