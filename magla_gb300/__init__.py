@@ -8,7 +8,7 @@ from .errors import (ArgumentException, ArgumentNullException, ArgumentOutOfRang
                      DeviceWaitTimeoutError, IndexOutOfRangeException, InvalidOperationException,
                      RefinementNotConvergedError)
 from .device_matrix import (AccumulatePlan, ConjugateGradientGaussPreSolver, DeviceSymmetricCSRMatrix,
-                            IterativeSolverResult, LineCrossPlan)
+                            IterativeSolverResult, JacobiPreconditioner, LineCrossPlan)
 from .matrix import LinearSystem, MatrixEntry, SymmetricCSRMatrix, SymmetricCSRMatrixBuilder
 from .solver import (BatchedUtduFactorization, BatchedUtduSolver, BatchedUtduSymbolic, DirectLinearSolver,
                      FillReducingOrdering, LinearSolver, Precision, ResidualCalculator, SymmetricUtduSolver,
@@ -21,5 +21,5 @@ __all__ = [
     "BatchedUtduFactorization", "BatchedUtduSolver", "BatchedUtduSymbolic", "FillReducingOrdering", "LinearSolver",
     "Precision", "ResidualCalculator", "SymmetricUtduSolver", "UtduNumericFactorization", "UtduSolverOptions",
     "UtduSymbolicFactorization", "AccumulatePlan", "ConjugateGradientGaussPreSolver", "DeviceSymmetricCSRMatrix",
-    "IterativeSolverResult", "LineCrossPlan",
+    "IterativeSolverResult", "JacobiPreconditioner", "LineCrossPlan",
 ]

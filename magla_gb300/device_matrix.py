@@ -12,6 +12,7 @@ include/uchol_gpu.h):
   (index lists: ``LineCrossPlan``)
 * ``DeviceSymmetricCSRMatrix.Multiply``      CAESolvers/SymmetricCSRMatrix.cs:259-324
 * ``ConjugateGradientGaussPreSolver``        CAESolvers/CGGP/ConjugateGradientGaussPreSolver.cs:40-197
+* ``JacobiPreconditioner``                   CAESolvers/CGGP/JacobiPreconditioner.cs:7-58
 * ``IterativeSolverResult``                  CAESolvers/CGGP/IterativeSolverResult.cs:8-40
 
 The values never need to leave the device between a refresh and a
@@ -245,6 +246,39 @@ class LineCrossPlan(_Plan):
                                        max(1, self.Count), 1))
 
 
+class JacobiPreconditioner:
+    """result = diag(A)^-1 source (CAESolvers/CGGP/JacobiPreconditioner.cs:7-58), built once for
+    a matrix.  Given to ConjugateGradientGaussPreSolver.SolveWithInitialGuess it takes priority
+    over UsePreconditioner; the device solver forms the inverse diagonal from the matrix's values
+    at solve time, the preconditioner's own as long as those values are unchanged."""
+
+    def __init__(self, matrix, pivotTolerance: float = 1e-300):
+        if matrix is None:
+            raise ArgumentNullException("matrix")
+        if not np.isfinite(pivotTolerance) or pivotTolerance <= 0.0:
+            raise ArgumentOutOfRangeException("pivotTolerance")
+        self.Matrix = matrix
+        self.PivotTolerance = pivotTolerance
+        self.Size = matrix.Size
+        diag = np.array([matrix.GetDiagonal(i) for i in range(self.Size)], np.float64) if self.Size else np.zeros(0)
+        bad = ~np.isfinite(diag) | (np.abs(diag) <= pivotTolerance)
+        if bad.any():
+            raise InvalidOperationException(f"The diagonal element in row {int(np.argmax(bad))} is zero or invalid "
+                                            "while building the Jacobi preconditioner.")
+        self._inverse = 1.0 / diag
+
+    def Apply(self, source, result) -> None:
+        if source is None:
+            raise ArgumentNullException("source")
+        if result is None:
+            raise ArgumentNullException("result")
+        if len(source) != self.Size:
+            raise ArgumentException("The source vector length does not match the preconditioner size.", "source")
+        if len(result) != self.Size:
+            raise ArgumentException("The result vector length does not match the preconditioner size.", "result")
+        result[:] = self._inverse * np.asarray(source, np.float64)
+
+
 class IterativeSolverResult:
     """CAESolvers/CGGP/IterativeSolverResult.cs:8-40."""
 
@@ -284,7 +318,9 @@ class ConjugateGradientGaussPreSolver:
     def Solve(self, system: LinearSystem) -> np.ndarray:
         return self.SolveWithInitialGuess(system, None)
 
-    def SolveWithInitialGuess(self, system: LinearSystem, initialGuess) -> np.ndarray:
+    def SolveWithInitialGuess(self, system: LinearSystem, initialGuess, preconditioner=None) -> np.ndarray:
+        """x0 = initialGuess (or 0); a given JacobiPreconditioner takes priority over
+        UsePreconditioner and must have been built for this system's matrix."""
         self.LastResult = None
         self._validate()
         if system is None:
@@ -293,12 +329,16 @@ class ConjugateGradientGaussPreSolver:
         n = matrix.Size
         if initialGuess is not None and len(initialGuess) != n:
             raise ArgumentException(f"The initial guess length {len(initialGuess)} does not match the matrix size {n}.")
+        if preconditioner is not None and preconditioner.Matrix is not matrix:
+            raise ArgumentException("The preconditioner was built for another matrix.", "preconditioner")
         dm = matrix if isinstance(matrix, DeviceSymmetricCSRMatrix) else DeviceSymmetricCSRMatrix(matrix)
         b = np.asfortranarray(np.asarray(system.RightHandSide, np.float64).reshape(n, -1))
         x = np.zeros_like(b, order="F") if initialGuess is None else \
             np.asfortranarray(np.asarray(initialGuess, np.float64).reshape(n, -1))
         res = (_native.CgResult * b.shape[1])()
         opts = self._options(initialGuess is not None)
+        if preconditioner is not None:
+            opts.use_preconditioner = 1
         ld = max(1, n)
         _check(_lib().uchol_jacobi_pcg(dm.handle, b.shape[1], _vp(b), ld, _vp(x), ld, 0, C.byref(opts), res))
         sol = x.reshape(np.shape(system.RightHandSide))
@@ -325,4 +365,4 @@ class ConjugateGradientGaussPreSolver:
 
 
 __all__ = ["DeviceSymmetricCSRMatrix", "AccumulatePlan", "LineCrossPlan", "ConjugateGradientGaussPreSolver",
-           "IterativeSolverResult", "InvalidOperationException"]
+           "JacobiPreconditioner", "IterativeSolverResult", "InvalidOperationException"]

@@ -305,3 +305,16 @@ def test_process_exit_with_live_handles(gpu_lib, tmp_path):
     r = subprocess.run([sys.executable, str(script)], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, (r.returncode, r.stderr[-2000:])
     assert "done" in r.stdout
+
+
+def test_pcg_provided_preconditioner_has_priority(gpu_lib):
+    """Tests/CGGP/JacobiPreconditionerTests.cs:38-54: a given preconditioner is reused and wins
+    over UsePreconditioner = False (one step each on a diagonal system)."""
+    from magla_gb300 import JacobiPreconditioner
+    m = _build(3, [(0, 0, 2.0), (1, 1, 4.0), (2, 2, 8.0)])
+    pre = JacobiPreconditioner(m)
+    s = ConjugateGradientGaussPreSolver(RelativeTolerance=1e-12, UsePreconditioner=False)
+    for expected in ([1.0, -2.0, 3.0], [-4.0, 5.0, 0.5]):
+        x = s.SolveWithInitialGuess(LinearSystem(m, oracle.multiply(m, np.array(expected))), None, pre)
+        assert s.LastResult.Iterations == 1
+        assert np.allclose(x, expected, rtol=0, atol=1e-12)

@@ -141,3 +141,25 @@ def test_device_cg_argument_checks_without_a_gpu():
         ConjugateGradientGaussPreSolver(RelativeTolerance=-1.0).Solve(LinearSystem(m, [1.0, 1.0]))
     with pytest.raises(ArgumentException):
         ConjugateGradientGaussPreSolver().SolveWithInitialGuess(LinearSystem(m, [1.0, 1.0]), [1.0])
+
+
+def test_jacobi_preconditioner_known_answers():
+    """Tests/CGGP/JacobiPreconditionerTests.cs:10-36, 57-65 (host mirror; no GPU)."""
+    from magla_gb300 import (ArgumentException, ConjugateGradientGaussPreSolver, InvalidOperationException,
+                             JacobiPreconditioner, LinearSystem)
+    p = JacobiPreconditioner(_diagonal([2.0, 4.0, 8.0]))
+    result = np.zeros(3)
+    p.Apply([4.0, 12.0, -8.0], result)
+    assert list(result) == [2.0, 3.0, -1.0]
+    with pytest.raises(InvalidOperationException):
+        JacobiPreconditioner(_diagonal([2.0, 0.0, 8.0]))
+    p2 = JacobiPreconditioner(_diagonal([2.0, 4.0]))
+    with pytest.raises(ArgumentException):
+        p2.Apply(np.zeros(1), np.zeros(2))
+    with pytest.raises(ArgumentException):
+        p2.Apply(np.zeros(2), np.zeros(1))
+    # a preconditioner built for another matrix (equal values, another object) is refused
+    m = _diagonal([2.0, 4.0])
+    with pytest.raises(ArgumentException):
+        ConjugateGradientGaussPreSolver().SolveWithInitialGuess(LinearSystem(m, [2.0, 4.0]), None,
+                                                               JacobiPreconditioner(_diagonal([2.0, 4.0])))
